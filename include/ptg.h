@@ -1,0 +1,169 @@
+/*
+ * ptg.h -- C ABI of the GB300-native CPD-ALS path (libptg.so).
+ *
+ * The reference (Partensor) exposes this path only through header-only C++ templates;
+ * its one extern "C" symbol is cuda_vecAdd (include/CUDA/add_vectors.cu:16-24).  The
+ * entry points below are what a binding for those templates needs: plain pointers,
+ * sizes and POD structs, no C++ or torch types.  Every function returns a ptg_status
+ * code; ptg_last_error() gives the message of the last failure on the calling thread.
+ *
+ * Data conventions (those of the reference):
+ *   - a dense tensor is ColMajor, i0 fastest (include/Tensor.hpp:64, Eigen::Tensor);
+ *   - a host factor matrix is I_k x R ColMajor FP64 (Eigen::MatrixXd, include/Tensor.hpp:42);
+ *   - device factor matrices used by the lower-level entry points are ROW-major FP32
+ *     [I_k][R] (element (i, r) at i*R + r), the layout the kernels read.
+ * Paths in the citations are relative to the reference project's root.
+ */
+#ifndef PTG_H
+#define PTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTG_MAX_ORDER 8
+
+typedef enum {
+  PTG_OK = 0,
+  PTG_ERR_INVALID = 1,     /* bad argument */
+  PTG_ERR_CUDA = 2,        /* a CUDA runtime/driver call failed */
+  PTG_ERR_OOM = 3,         /* device allocation failed */
+  PTG_ERR_UNSUPPORTED = 4, /* shape/rank outside what the kernels handle */
+  PTG_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  PTG_ERR_NUMERIC = 6      /* NaN/Inf detected in an input or a result */
+} ptg_status;
+
+typedef enum { PTG_F32 = 0, PTG_BF16 = 1 } ptg_dtype;
+
+/* Constraint values of include/Constants.hpp:49-57. */
+typedef enum {
+  PTG_UNCONSTRAINED = 0,
+  PTG_NONNEGATIVITY = 1,
+  PTG_ORTHOGONALITY = 2,
+  PTG_SPARSITY = 3,
+  PTG_CONSTANT = 4
+} ptg_constraint;
+
+typedef struct ptg_ctx ptg_ctx;
+typedef struct ptg_tensor ptg_tensor;
+
+/* Text of the last error raised on this thread ("" if none). */
+const char *ptg_last_error(void);
+
+/* Library version string. */
+const char *ptg_version(void);
+
+/* One context per device and caller thread: owns streams, events and workspace.
+ * Replaces the per-call cublasCreate/cudaStreamCreate/cudaMallocManaged set-up of
+ * include/CUDA/CpdCUDA.hpp:282-300. */
+int ptg_ctx_create(int device, ptg_ctx **out);
+int ptg_ctx_destroy(ptg_ctx *ctx);
+/* Run all work of this context on a caller-provided cudaStream_t (NULL: own stream). */
+int ptg_ctx_set_stream(ptg_ctx *ctx, void *cuda_stream);
+int ptg_ctx_synchronize(ptg_ctx *ctx);
+
+/* Kernel statistics of a context (no counterpart in the reference, which only has a
+ * host stopwatch, include/Timers.hpp:39-142).  When enabled, every MTTKRP launch is
+ * bracketed by CUDA events on the stream it runs on. */
+typedef struct {
+  long long launches;         /* all kernels this context launched */
+  long long mttkrp_launches;  /* MTTKRP contractions (main kernel + split-K reduction) */
+  double mttkrp_ms;           /* summed event time of those contractions */
+  double mttkrp_bytes;        /* algorithmic bytes: tensor + factors read, result written */
+  double mttkrp_flops;        /* 2 * prod(I) * R per contraction */
+} ptg_stats;
+int ptg_ctx_enable_stats(ptg_ctx *ctx, int enable);
+int ptg_ctx_get_stats(ptg_ctx *ctx, ptg_stats *out); /* synchronises the context's stream */
+int ptg_ctx_reset_stats(ptg_ctx *ctx);
+
+/* Dense tensor resident in HBM in the requested storage type.  src is an FP64 ColMajor
+ * buffer with prod(dims) entries, on the host (src_on_device = 0) or on the device.
+ * Replaces the host Matricization copies of include/CUDA/CpdCUDA.hpp:302-306: the
+ * tensor is stored once, in its natural order, with mode 0 padded to a multiple of 8
+ * (pads are zero).  ||X||^2 (include/TensorOperations.hpp:144-149) is computed in FP64
+ * from the FP64 source during the upload. */
+int ptg_tensor_create(ptg_ctx *ctx, int order, const int64_t *dims, ptg_dtype dtype,
+                      const double *src, int src_on_device, ptg_tensor **out);
+int ptg_tensor_destroy(ptg_tensor *t);
+/* frob64: ||X||^2 of the FP64 source; frob_stored: ||X||^2 of the stored (rounded) copy. */
+int ptg_tensor_norms(const ptg_tensor *t, double *frob64, double *frob_stored);
+
+/* Mode-n MTTKRP, M = X_(n) * KhatriRao_{k != n}(A_k).  Replaces mttkrp
+ * (include/MTTKRP.hpp:60-69, 102-225) and hybrid_batched_mttkrp
+ * (include/CUDA/CUDAMTTKRP.hpp:67-200).  factors[k]: device, row-major FP32 [I_k][R]
+ * (factors[mode] is not read).  out: device, row-major FP32 [I_mode][R].
+ * Asynchronous on the context's stream. */
+int ptg_mttkrp(ptg_ctx *ctx, const ptg_tensor *X, const float *const *factors, int rank, int mode,
+               float *out);
+
+/* Options of one CPD-ALS run: the fields of partensor::Options
+ * (include/PARTENSOR_basic.hpp:283-336) that the ALS loop reads, plus GB300 knobs. */
+typedef struct {
+  int constraints[PTG_MAX_ORDER];
+  double threshold_error;
+  double nesterov_delta_1;
+  double nesterov_delta_2;
+  int max_iter;
+  int accel_coeff;
+  int accel_fail;
+  int acceleration;
+  int normalization;
+  /* GB300 extensions (Gb300Options): */
+  int refine_sweeps; /* FP32 sweeps run on `refine` after the main loop stops (0: none) */
+  int warm_start;    /* 1: MLP warm start for the NNLS rows (needs a trained model) */
+  int cost_every_sweep; /* reserved, must be 1 */
+} ptg_cpd_options;
+
+/* Fill *o with the reference defaults (include/PARTENSOR_basic.hpp:176-218). */
+void ptg_cpd_default_options(int order, ptg_cpd_options *o);
+
+/* Scalars of partensor::Status (include/PARTENSOR_basic.hpp:556-595) plus timing. */
+typedef struct {
+  double frob_tns;
+  double f_value;
+  double rel_costFunction;
+  int ao_iter;
+  int accel_coeff;
+  int accel_fail;
+  int refine_sweeps_done;
+  long long nesterov_iters_total;
+  double seconds_total;
+} ptg_cpd_result;
+
+/* Per-sweep trace record (optional output). */
+typedef struct {
+  double f_value;          /* cost after the sweep, before acceleration */
+  double rel_costFunction;
+  double f_accel;          /* cost of the accelerated point (0 when not tried) */
+  int accel_accepted;
+  int nesterov_iters[PTG_MAX_ORDER];
+  float seconds;           /* wall time since the start of the run */
+} ptg_sweep_trace;
+
+/* CPD-ALS on a resident tensor: the loop of include/Cpd.hpp:288-356 /
+ * include/CUDA/CpdCUDA.hpp:277-383 with all per-iteration work on the GPU.
+ *   X       the tensor the main loop uses (FP32 or BF16 storage);
+ *   refine  optional FP32 copy for the refinement sweeps (may be NULL);
+ *   init_factors[k]: host FP64 ColMajor I_k x R (the factorsInit overloads,
+ *           include/Cpd.hpp:534-577);
+ *   out_factors[k]:  host FP64 ColMajor I_k x R (may alias init_factors);
+ *   trace (optional) holds max_iter + refine_sweeps records. */
+int ptg_cpd_als(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int rank,
+                const ptg_cpd_options *opts, const double *const *init_factors,
+                double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace);
+
+/* One-call form with a HOST FP64 tensor: upload (with conversion to `dtype`), solve,
+ * download.  This is what partensor::cpd(execution::cuda, tnsX, R, options, factorsInit)
+ * (include/Cpd.hpp:1116-1144) binds to. */
+int ptg_cpd(ptg_ctx *ctx, int order, const int64_t *dims, const double *host_tensor,
+            ptg_dtype dtype, int rank, const ptg_cpd_options *opts,
+            const double *const *init_factors, double *const *out_factors,
+            ptg_cpd_result *result, ptg_sweep_trace *trace);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PTG_H */

@@ -1,0 +1,250 @@
+"""Host-side mirror of Partensor's dense CPD interface on top of libptg.
+
+``cpd(tnsX, R, options, factorsInit)`` follows ``partensor::cpd(execution::cuda, ...)``
+(include/Cpd.hpp:893-1171): same argument meaning, same ``Options`` fields and defaults
+(include/PARTENSOR_basic.hpp:176-218, 283-336), a ``Status`` with the fields of
+include/PARTENSOR_basic.hpp:556-595.  Tensors are float64 in ColMajor order (a numpy
+array with ``order='F'`` of shape dims, or a flat buffer plus ``dims``); factor matrices
+are I_k x R float64.  All compute runs in libptg on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import CpdOptions, CpdResult, SweepTrace, check
+
+UNCONSTRAINED, NONNEGATIVITY, ORTHOGONALITY, SPARSITY, CONSTANT = 0, 1, 2, 3, 4
+DTYPES = {"f32": _lib.PTG_F32, "fp32": _lib.PTG_F32, "bf16": _lib.PTG_BF16}
+
+
+@dataclasses.dataclass
+class Options:
+    """partensor::Options (include/PARTENSOR_basic.hpp:283-336) plus the GB300 knobs."""
+    order: int = 3
+    constraints: Optional[List[int]] = None
+    threshold_error: float = 1e-3
+    nesterov_delta_1: float = 1e-2
+    nesterov_delta_2: float = 1e-2
+    max_iter: int = 20
+    accel_coeff: int = 3
+    accel_fail: int = 0
+    acceleration: bool = True
+    normalization: bool = True
+    # GB300 extensions
+    precision: str = "f32"        # storage of the tensor in HBM: "f32" or "bf16"
+    refine_sweeps: int = 0        # FP32 sweeps after the main loop (bf16 storage only)
+    warm_start: bool = False
+
+    def __post_init__(self):
+        if self.constraints is None:
+            self.constraints = [NONNEGATIVITY] * self.order
+
+    def to_c(self) -> CpdOptions:
+        o = CpdOptions()
+        _lib.load().ptg_cpd_default_options(self.order, ctypes.byref(o))
+        for k in range(self.order):
+            o.constraints[k] = int(self.constraints[k])
+        o.threshold_error = self.threshold_error
+        o.nesterov_delta_1 = self.nesterov_delta_1
+        o.nesterov_delta_2 = self.nesterov_delta_2
+        o.max_iter = int(self.max_iter)
+        o.accel_coeff = int(self.accel_coeff)
+        o.accel_fail = int(self.accel_fail)
+        o.acceleration = int(bool(self.acceleration))
+        o.normalization = int(bool(self.normalization))
+        o.refine_sweeps = int(self.refine_sweeps)
+        o.warm_start = int(bool(self.warm_start))
+        return o
+
+
+@dataclasses.dataclass
+class Status:
+    """partensor::Status (include/PARTENSOR_basic.hpp:556-595) plus a per-sweep trace."""
+    options: Options
+    factors: List[np.ndarray]
+    frob_tns: float = 0.0
+    f_value: float = 0.0
+    rel_costFunction: float = 0.0
+    ao_iter: int = 0
+    refine_sweeps_done: int = 0
+    nesterov_iters_total: int = 0
+    seconds: float = 0.0
+    trace: list = dataclasses.field(default_factory=list)
+
+
+class Context:
+    """A libptg context on one device (streams, events, workspace)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(self._lib.ptg_ctx_create(int(device), ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def set_stream(self, stream_ptr: int | None):
+        check(self._lib.ptg_ctx_set_stream(self.handle, ctypes.c_void_p(stream_ptr or 0)))
+
+    def synchronize(self):
+        check(self._lib.ptg_ctx_synchronize(self.handle))
+
+    def enable_stats(self, on: bool = True):
+        check(self._lib.ptg_ctx_enable_stats(self.handle, int(on)))
+
+    def reset_stats(self):
+        check(self._lib.ptg_ctx_reset_stats(self.handle))
+
+    def stats(self) -> dict:
+        s = _lib.Stats()
+        check(self._lib.ptg_ctx_get_stats(self.handle, ctypes.byref(s)))
+        return dict(launches=s.launches, mttkrp_launches=s.mttkrp_launches, mttkrp_ms=s.mttkrp_ms,
+                    mttkrp_bytes=s.mttkrp_bytes, mttkrp_flops=s.mttkrp_flops)
+
+    def close(self):
+        if self.handle:
+            self._lib.ptg_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Optional[Context] = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Tensor:
+    """A dense tensor resident in HBM (``ptg_tensor_create``).
+
+    ``src`` is either a float64 numpy array (ColMajor: Fortran-ordered of shape ``dims``,
+    or flat with ``dims`` given) or a ``(device_pointer, dims)`` pair of a float64
+    ColMajor buffer already on the GPU."""
+
+    def __init__(self, ctx: Context, src, dims: Sequence[int] | None = None, precision: str = "f32"):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        if isinstance(src, tuple):
+            ptr, dims = src
+            on_dev, p = 1, ctypes.cast(ctypes.c_void_p(int(ptr)), ctypes.POINTER(ctypes.c_double))
+            self._keep = None
+        else:
+            a = np.asarray(src, dtype=np.float64)
+            if dims is None:
+                dims = a.shape
+                a = np.asfortranarray(a).reshape(-1, order="F")
+            else:
+                a = np.ascontiguousarray(a.reshape(-1))
+            on_dev, p = 0, _dptr(a)
+            self._keep = a
+        self.dims = [int(d) for d in dims]
+        self.precision = precision
+        d = (ctypes.c_int64 * len(self.dims))(*self.dims)
+        h = ctypes.c_void_p()
+        check(self._lib.ptg_tensor_create(ctx.handle, len(self.dims), d, DTYPES[precision], p, on_dev,
+                                          ctypes.byref(h)))
+        self.handle = h
+        self._keep = None
+
+    def norms(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        check(self._lib.ptg_tensor_norms(self.handle, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.ptg_tensor_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mttkrp(ctx: Context, X: Tensor, factor_ptrs: Sequence[int], rank: int, mode: int, out_ptr: int):
+    """Device-level MTTKRP (``ptg_mttkrp``): factor_ptrs are device pointers to row-major
+    FP32 [I_k][R] matrices, out_ptr a device row-major FP32 [I_mode][R] buffer."""
+    arr = (ctypes.c_void_p * len(factor_ptrs))(*[ctypes.c_void_p(int(p)) for p in factor_ptrs])
+    check(ctx._lib.ptg_mttkrp(ctx.handle, X.handle, arr, int(rank), int(mode), ctypes.c_void_p(int(out_ptr))))
+
+
+def _status_from(opts: Options, outs, res: CpdResult, trace, ntrace) -> Status:
+    st = Status(options=opts, factors=outs, frob_tns=res.frob_tns, f_value=res.f_value,
+                rel_costFunction=res.rel_costFunction, ao_iter=res.ao_iter,
+                refine_sweeps_done=res.refine_sweeps_done,
+                nesterov_iters_total=int(res.nesterov_iters_total), seconds=res.seconds_total)
+    st.options = dataclasses.replace(opts, accel_coeff=res.accel_coeff, accel_fail=res.accel_fail)
+    for i in range(ntrace):
+        t = trace[i]
+        st.trace.append(dict(f_value=t.f_value, rel=t.rel_costFunction, f_accel=t.f_accel,
+                             accel_accepted=bool(t.accel_accepted),
+                             nesterov_iters=list(t.nesterov_iters)[:opts.order], seconds=t.seconds))
+    return st
+
+
+def cpd_resident(ctx: Context, X: Tensor, R: int, options: Options, factorsInit: Sequence[np.ndarray],
+                 refine: Optional[Tensor] = None) -> Status:
+    """CPD-ALS on an HBM-resident tensor (``ptg_cpd_als``)."""
+    N = len(X.dims)
+    inits = [np.asfortranarray(np.asarray(f, dtype=np.float64)) for f in factorsInit]
+    outs = [np.zeros((X.dims[k], R), order="F") for k in range(N)]
+    ip = (ctypes.POINTER(ctypes.c_double) * N)(*[_dptr(a) for a in inits])
+    op = (ctypes.POINTER(ctypes.c_double) * N)(*[_dptr(a) for a in outs])
+    res = CpdResult()
+    ntr = options.max_iter + max(0, options.refine_sweeps)
+    trace = (SweepTrace * ntr)()
+    check(ctx._lib.ptg_cpd_als(ctx.handle, X.handle, refine.handle if refine else None, int(R),
+                               ctypes.byref(options.to_c()), ip, op, ctypes.byref(res), trace))
+    return _status_from(options, outs, res, trace, res.ao_iter + res.refine_sweeps_done)
+
+
+def cpd(tnsX, R: int, options: Optional[Options] = None, factorsInit: Optional[Sequence[np.ndarray]] = None,
+        dims: Sequence[int] | None = None, ctx: Optional[Context] = None) -> Status:
+    """partensor::cpd(execution::cuda, tnsX, R[, options][, factorsInit]) with a host
+    FP64 tensor (``ptg_cpd``: upload, convert, solve, download in one call).
+
+    Without ``factorsInit`` the initial factors are U[0,1] like makeFactors
+    (include/DataGeneration.hpp:564-581) but from a seeded generator."""
+    ctx = ctx or default_context()
+    a = np.asarray(tnsX, dtype=np.float64)
+    if dims is None:
+        dims = a.shape
+        flat = np.asfortranarray(a).reshape(-1, order="F")
+    else:
+        flat = np.ascontiguousarray(a.reshape(-1))
+    dims = [int(d) for d in dims]
+    N = len(dims)
+    options = options or Options(order=N)
+    if factorsInit is None:
+        rng = np.random.default_rng(0)
+        factorsInit = [rng.random((I, R)) for I in dims]
+    inits = [np.asfortranarray(np.asarray(f, dtype=np.float64)) for f in factorsInit]
+    outs = [np.zeros((dims[k], R), order="F") for k in range(N)]
+    ip = (ctypes.POINTER(ctypes.c_double) * N)(*[_dptr(x) for x in inits])
+    op = (ctypes.POINTER(ctypes.c_double) * N)(*[_dptr(x) for x in outs])
+    d = (ctypes.c_int64 * N)(*dims)
+    res = CpdResult()
+    ntr = options.max_iter + max(0, options.refine_sweeps)
+    trace = (SweepTrace * ntr)()
+    check(ctx._lib.ptg_cpd(ctx.handle, N, d, _dptr(flat), DTYPES[options.precision], int(R),
+                           ctypes.byref(options.to_c()), ip, op, ctypes.byref(res), trace))
+    return _status_from(options, outs, res, trace, res.ao_iter + res.refine_sweeps_done)

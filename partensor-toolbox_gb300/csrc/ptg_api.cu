@@ -1,0 +1,416 @@
+// C ABI: errors, contexts, resident tensors, MTTKRP.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ptg_internal.h"
+
+namespace ptg {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char *what, const char *file, int line) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+  return set_error(e == cudaErrorMemoryAllocation ? PTG_ERR_OOM : PTG_ERR_CUDA, buf);
+}
+
+int DevBuf::ensure(size_t need) {
+  if (need <= bytes) return PTG_OK;
+  if (ptr) {
+    cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  size_t sz = std::max(need, (size_t)1 << 20);
+  cudaError_t e = cudaMalloc(&ptr, sz);
+  if (e != cudaSuccess) {
+    ptr = nullptr;
+    return cuda_error(e, "cudaMalloc(scratch)", __FILE__, __LINE__);
+  }
+  bytes = sz;
+  return PTG_OK;
+}
+
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+int stats_begin(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t *ev) {
+  *ev = nullptr;
+  if (!ctx->stats.enabled) return PTG_OK;
+  if (ctx->stats.pool.empty()) {
+    cudaEvent_t e;
+    PTG_CUDA(cudaEventCreate(&e));
+    ctx->stats.pool.push_back(e);
+  }
+  *ev = ctx->stats.pool.back();
+  ctx->stats.pool.pop_back();
+  PTG_CUDA(cudaEventRecord(*ev, s));
+  return PTG_OK;
+}
+
+int stats_end(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t ev0, double bytes, double flops) {
+  if (!ctx->stats.enabled || !ev0) return PTG_OK;
+  cudaEvent_t ev1;
+  if (ctx->stats.pool.empty()) {
+    PTG_CUDA(cudaEventCreate(&ev1));
+  } else {
+    ev1 = ctx->stats.pool.back();
+    ctx->stats.pool.pop_back();
+  }
+  PTG_CUDA(cudaEventRecord(ev1, s));
+  ctx->stats.pending.emplace_back(ev0, ev1);
+  ctx->stats.mttkrp_launches++;
+  ctx->stats.mttkrp_bytes += bytes;
+  ctx->stats.mttkrp_flops += flops;
+  return PTG_OK;
+}
+
+int stats_resolve(ptg_ctx *ctx) {
+  for (auto &pr : ctx->stats.pending) {
+    PTG_CUDA(cudaEventSynchronize(pr.second));
+    float ms = 0.f;
+    PTG_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+    ctx->stats.mttkrp_ms += ms;
+    ctx->stats.pool.push_back(pr.first);
+    ctx->stats.pool.push_back(pr.second);
+  }
+  ctx->stats.pending.clear();
+  return PTG_OK;
+}
+
+namespace {
+
+// FP64 ColMajor source chunk -> padded storage, with FP64 partial sums of squares of the
+// source and of the stored values (one pair per block, summed later in block order).
+template <typename T>
+__device__ __forceinline__ T cvt(double x);
+template <>
+__device__ __forceinline__ float cvt<float>(double x) { return (float)x; }
+template <>
+__device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16>(double x) { return __double2bfloat16(x); }
+__device__ __forceinline__ double back(float x) { return (double)x; }
+__device__ __forceinline__ double back(__nv_bfloat16 x) { return (double)__bfloat162float(x); }
+
+constexpr int kConvBlocks = 1024;
+constexpr int kConvThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kConvThreads)
+convert_kernel(const double *__restrict__ src, int64_t I0, int64_t pI0, int64_t fiber0,
+               int64_t nfibers, T *__restrict__ dst, double *__restrict__ part) {
+  // element e of the padded chunk: i0 = e % pI0, fiber = e / pI0
+  const int64_t n = nfibers * pI0;
+  double s64 = 0.0, sst = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i0 = e % pI0, f = e / pI0;
+    T v;
+    if (i0 < I0) {
+      const double x = src[f * I0 + i0];
+      v = cvt<T>(x);
+      s64 = fma(x, x, s64);
+      const double b = back(v);
+      sst = fma(b, b, sst);
+    } else {
+      v = cvt<T>(0.0);
+    }
+    dst[(fiber0 + f) * pI0 + i0] = v;
+  }
+  __shared__ double r64[kConvThreads / 32], rst[kConvThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    s64 += __shfl_down_sync(0xffffffffu, s64, o);
+    sst += __shfl_down_sync(0xffffffffu, sst, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    r64[threadIdx.x >> 5] = s64;
+    rst[threadIdx.x >> 5] = sst;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < kConvThreads / 32; ++w) {
+      a += r64[w];
+      b += rst[w];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+
+__global__ void sum_partials_kernel(const double *part, int nblocks, double *acc) {
+  // single thread, fixed order: deterministic
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double a = acc[0], b = acc[1];
+    for (int i = 0; i < nblocks; ++i) {
+      a += part[2 * i];
+      b += part[2 * i + 1];
+    }
+    acc[0] = a;
+    acc[1] = b;
+  }
+}
+
+}  // namespace
+}  // namespace ptg
+
+using namespace ptg;
+
+extern "C" {
+
+const char *ptg_last_error(void) { return g_last_error.c_str(); }
+
+const char *ptg_version(void) { return "ptg 0.1 (sm_103a)"; }
+
+int ptg_ctx_create(int device, ptg_ctx **out) {
+  if (!out) return set_error(PTG_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  PTG_CUDA(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return set_error(PTG_ERR_INVALID, "no such device");
+  PTG_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  PTG_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (prop.major < 10)
+    return set_error(PTG_ERR_UNSUPPORTED, "libptg is built for sm_103a (GB300) only");
+  ptg_ctx *c = new ptg_ctx();
+  c->device = device;
+  c->sm_count = prop.multiProcessorCount;
+  c->cc_major = prop.major;
+  c->cc_minor = prop.minor;
+  c->smem_optin = prop.sharedMemPerBlockOptin;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    ptg_ctx_destroy(c);
+    return cuda_error(e, "ptg_ctx_create", __FILE__, __LINE__);
+  }
+  c->stream = c->own_stream;
+  *out = c;
+  return PTG_OK;
+}
+
+int ptg_ctx_destroy(ptg_ctx *c) {
+  if (!c) return PTG_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->scratch.release();
+  stats_resolve(c);
+  for (cudaEvent_t e : c->stats.pool) cudaEventDestroy(e);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->side) cudaStreamDestroy(c->side);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+  return PTG_OK;
+}
+
+int ptg_ctx_set_stream(ptg_ctx *c, void *s) {
+  if (!c) return set_error(PTG_ERR_INVALID, "ctx is NULL");
+  c->stream = s ? (cudaStream_t)s : c->own_stream;
+  return PTG_OK;
+}
+
+int ptg_ctx_synchronize(ptg_ctx *c) {
+  if (!c) return set_error(PTG_ERR_INVALID, "ctx is NULL");
+  PTG_CUDA(cudaSetDevice(c->device));
+  PTG_CUDA(cudaStreamSynchronize(c->stream));
+  return PTG_OK;
+}
+
+int ptg_ctx_enable_stats(ptg_ctx *c, int enable) {
+  if (!c) return set_error(PTG_ERR_INVALID, "ctx is NULL");
+  c->stats.enabled = enable != 0;
+  return PTG_OK;
+}
+
+int ptg_ctx_get_stats(ptg_ctx *c, ptg_stats *out) {
+  if (!c || !out) return set_error(PTG_ERR_INVALID, "NULL argument");
+  PTG_CUDA(cudaSetDevice(c->device));
+  PTG_CUDA(cudaStreamSynchronize(c->stream));
+  PTG_TRY(stats_resolve(c));
+  out->launches = c->stats.launches;
+  out->mttkrp_launches = c->stats.mttkrp_launches;
+  out->mttkrp_ms = c->stats.mttkrp_ms;
+  out->mttkrp_bytes = c->stats.mttkrp_bytes;
+  out->mttkrp_flops = c->stats.mttkrp_flops;
+  return PTG_OK;
+}
+
+int ptg_ctx_reset_stats(ptg_ctx *c) {
+  if (!c) return set_error(PTG_ERR_INVALID, "ctx is NULL");
+  PTG_CUDA(cudaSetDevice(c->device));
+  PTG_CUDA(cudaStreamSynchronize(c->stream));
+  PTG_TRY(stats_resolve(c));
+  const bool en = c->stats.enabled;
+  c->stats.launches = c->stats.mttkrp_launches = 0;
+  c->stats.mttkrp_ms = c->stats.mttkrp_bytes = c->stats.mttkrp_flops = 0.0;
+  c->stats.enabled = en;
+  return PTG_OK;
+}
+
+int ptg_tensor_create(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtype,
+                      const double *src, int src_on_device, ptg_tensor **out) {
+  if (!c || !dims || !src || !out) return set_error(PTG_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (order < 2 || order > PTG_MAX_ORDER)
+    return set_error(PTG_ERR_UNSUPPORTED, "tensor order must be in [2, 8]");
+  if (dtype != PTG_F32 && dtype != PTG_BF16) return set_error(PTG_ERR_UNSUPPORTED, "dtype");
+  int64_t numel = 1;
+  for (int k = 0; k < order; ++k) {
+    if (dims[k] < 1 || dims[k] > 0x7fffffffLL)
+      return set_error(PTG_ERR_INVALID, "every dimension must be in [1, 2^31)");
+    numel *= dims[k];
+  }
+  PTG_CUDA(cudaSetDevice(c->device));
+  ptg_tensor *t = new ptg_tensor();
+  t->order = order;
+  for (int k = 0; k < order; ++k) t->dims[k] = dims[k];
+  t->pdim0 = (dims[0] + 7) / 8 * 8;
+  t->numel_padded = numel / dims[0] * t->pdim0;
+  t->dtype = dtype;
+  t->device = c->device;
+  const size_t esz = dtype == PTG_F32 ? 4 : 2;
+  cudaError_t e = cudaMalloc(&t->data, (size_t)t->numel_padded * esz);
+  if (e != cudaSuccess) {
+    delete t;
+    return cuda_error(e, "cudaMalloc(tensor)", __FILE__, __LINE__);
+  }
+  const int64_t I0 = dims[0], pI0 = t->pdim0;
+  const int64_t nfib = numel / I0;
+  // staging for host sources: two chunk buffers, copies on `side`, conversion on `stream`
+  const int64_t chunk_fib = std::max<int64_t>(1, std::min<int64_t>(nfib, (64ll << 20) / I0));
+  double *stage[2] = {nullptr, nullptr};
+  double *part = nullptr, *acc = nullptr;
+  cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+  int rc = PTG_OK;
+  auto fail = [&](int code) {
+    rc = code;
+    return code;
+  };
+  do {
+    if ((e = cudaMalloc(&part, sizeof(double) * 2 * kConvBlocks)) != cudaSuccess) {
+      fail(cuda_error(e, "cudaMalloc", __FILE__, __LINE__));
+      break;
+    }
+    if ((e = cudaMalloc(&acc, sizeof(double) * 2)) != cudaSuccess) {
+      fail(cuda_error(e, "cudaMalloc", __FILE__, __LINE__));
+      break;
+    }
+    cudaMemsetAsync(acc, 0, sizeof(double) * 2, c->stream);
+    if (!src_on_device) {
+      for (int b = 0; b < 2 && rc == PTG_OK; ++b) {
+        if ((e = cudaMalloc(&stage[b], sizeof(double) * chunk_fib * I0)) != cudaSuccess)
+          fail(cuda_error(e, "cudaMalloc(stage)", __FILE__, __LINE__));
+        else if ((e = cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming)) != cudaSuccess ||
+                 (e = cudaEventCreateWithFlags(&consumed[b], cudaEventDisableTiming)) != cudaSuccess)
+          fail(cuda_error(e, "cudaEventCreate", __FILE__, __LINE__));
+      }
+      if (rc != PTG_OK) break;
+    }
+    int chunk_idx = 0;
+    for (int64_t f0 = 0; f0 < nfib; f0 += chunk_fib, ++chunk_idx) {
+      const int64_t nf = std::min(chunk_fib, nfib - f0);
+      const double *csrc;
+      if (src_on_device) {
+        csrc = src + f0 * I0;
+      } else {
+        const int b = chunk_idx & 1;
+        if (chunk_idx >= 2) cudaStreamWaitEvent(c->side, consumed[b], 0);
+        e = cudaMemcpyAsync(stage[b], src + f0 * I0, sizeof(double) * nf * I0,
+                            cudaMemcpyHostToDevice, c->side);
+        if (e != cudaSuccess) {
+          fail(cuda_error(e, "cudaMemcpyAsync(H2D)", __FILE__, __LINE__));
+          break;
+        }
+        cudaEventRecord(copied[b], c->side);
+        cudaStreamWaitEvent(c->stream, copied[b], 0);
+        csrc = stage[b];
+      }
+      const int64_t n = nf * pI0;
+      const int blocks = (int)std::min<int64_t>(kConvBlocks, (n + kConvThreads - 1) / kConvThreads);
+      if (dtype == PTG_F32)
+        convert_kernel<float><<<blocks, kConvThreads, 0, c->stream>>>(
+            csrc, I0, pI0, f0, nf, (float *)t->data, part);
+      else
+        convert_kernel<__nv_bfloat16><<<blocks, kConvThreads, 0, c->stream>>>(
+            csrc, I0, pI0, f0, nf, (__nv_bfloat16 *)t->data, part);
+      sum_partials_kernel<<<1, 32, 0, c->stream>>>(part, blocks, acc);
+      count_launches(c, 2);
+      if (!src_on_device) cudaEventRecord(consumed[chunk_idx & 1], c->stream);
+      if ((e = cudaGetLastError()) != cudaSuccess) {
+        fail(cuda_error(e, "convert_kernel", __FILE__, __LINE__));
+        break;
+      }
+    }
+    if (rc != PTG_OK) break;
+    double h[2];
+    e = cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+      fail(cuda_error(e, "ptg_tensor_create", __FILE__, __LINE__));
+      break;
+    }
+    t->frob64 = h[0];
+    t->frob_stored = h[1];
+    if (!std::isfinite(h[0]) || !std::isfinite(h[1]))
+      fail(set_error(PTG_ERR_NUMERIC, "tensor contains NaN or Inf"));
+  } while (0);
+  if (src_on_device == 0) cudaStreamSynchronize(c->side);
+  for (int b = 0; b < 2; ++b) {
+    if (stage[b]) cudaFree(stage[b]);
+    if (copied[b]) cudaEventDestroy(copied[b]);
+    if (consumed[b]) cudaEventDestroy(consumed[b]);
+  }
+  if (part) cudaFree(part);
+  if (acc) cudaFree(acc);
+  if (rc != PTG_OK) {
+    cudaFree(t->data);
+    delete t;
+    return rc;
+  }
+  *out = t;
+  return PTG_OK;
+}
+
+int ptg_tensor_destroy(ptg_tensor *t) {
+  if (!t) return PTG_OK;
+  cudaSetDevice(t->device);
+  if (t->data) cudaFree(t->data);
+  delete t;
+  return PTG_OK;
+}
+
+int ptg_tensor_norms(const ptg_tensor *t, double *frob64, double *frob_stored) {
+  if (!t) return set_error(PTG_ERR_INVALID, "tensor is NULL");
+  if (frob64) *frob64 = t->frob64;
+  if (frob_stored) *frob_stored = t->frob_stored;
+  return PTG_OK;
+}
+
+int ptg_mttkrp(ptg_ctx *c, const ptg_tensor *X, const float *const *factors, int rank, int mode,
+               float *out) {
+  if (!c || !X || !factors || !out) return set_error(PTG_ERR_INVALID, "NULL argument");
+  if (mode < 0 || mode >= X->order) return set_error(PTG_ERR_INVALID, "mode out of range");
+  if (rank < 1) return set_error(PTG_ERR_INVALID, "rank must be >= 1");
+  for (int k = 0; k < X->order; ++k)
+    if (k != mode && !factors[k]) return set_error(PTG_ERR_INVALID, "factor pointer is NULL");
+  PTG_CUDA(cudaSetDevice(c->device));
+  Contraction con = mttkrp_contraction(X, factors, mode);
+  return contraction_launch(c, X, con, rank, out, c->stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+// Internal declarations shared by the translation units of libptg.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "ptg.h"
+
+namespace ptg {
+
+// ---------------------------------------------------------------------------------
+// Errors: every C entry point returns a ptg_status; the message is kept per thread.
+// ---------------------------------------------------------------------------------
+int set_error(int code, const std::string &msg);
+int cuda_error(cudaError_t e, const char *what, const char *file, int line);
+
+#define PTG_CUDA(call)                                                          \
+  do {                                                                          \
+    cudaError_t _e = (call);                                                    \
+    if (_e != cudaSuccess) return ::ptg::cuda_error(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define PTG_TRY(...)                   \
+  do {                                 \
+    int _s = (__VA_ARGS__);            \
+    if (_s != PTG_OK) return _s;       \
+  } while (0)
+
+// Device buffer that grows on demand (never shrinks until the context dies).
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need);
+  void release();
+};
+
+}  // namespace ptg
+
+struct ptg_ctx_stats {
+  bool enabled = false;
+  long long launches = 0;
+  long long mttkrp_launches = 0;
+  double mttkrp_ms = 0.0, mttkrp_bytes = 0.0, mttkrp_flops = 0.0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;   // unresolved event pairs
+  std::vector<cudaEvent_t> pool;
+};
+
+struct ptg_ctx {
+  int device = 0;
+  int sm_count = 0;
+  int cc_major = 0, cc_minor = 0;
+  size_t smem_optin = 0;
+  cudaStream_t stream = nullptr;      // main stream (own or caller's)
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t side = nullptr;        // concurrent small kernels (FP64 eigenbounds)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  ptg::DevBuf scratch;                // split-K partials and other temporaries
+  int nnls_cluster = 0;               // cluster size the NNLS kernel launched with (0 = unknown)
+  ptg_ctx_stats stats;
+};
+
+struct ptg_tensor {
+  int order = 0;
+  int64_t dims[PTG_MAX_ORDER] = {0};
+  int64_t pdim0 = 0;   // mode-0 extent padded to a multiple of 8 (pads are zero)
+  int64_t numel_padded = 0;
+  ptg_dtype dtype = PTG_F32;
+  void *data = nullptr;
+  double frob64 = 0.0;      // ||X||^2 of the FP64 source
+  double frob_stored = 0.0; // ||X||^2 of the stored copy
+  int device = 0;
+};
+
+namespace ptg {
+
+// Description of one MTTKRP-shaped contraction over the tensor viewed as [P, Q, S]:
+//   out[q, r] = sum_{p, s} X[p + P*q + P*Q*s] * KRb[p, r] * KRa[s, r]
+// KRb is the Khatri-Rao row of the factors of the modes before q (digits of p, fastest
+// first); KRa that of the modes after q (digits of s, fastest first).
+struct KrSide {
+  int n = 0;                            // number of factors
+  int64_t ext[PTG_MAX_ORDER] = {0};     // extent of each digit (padded extent for mode 0)
+  int64_t valid[PTG_MAX_ORDER] = {0};   // rows that exist (digit >= valid -> KR value 0)
+  const float *fac[PTG_MAX_ORDER] = {nullptr};  // row-major [valid][R]
+};
+
+struct Contraction {
+  int64_t P = 1, Q = 1, S = 1;
+  KrSide before, after;
+  int64_t q_write = 0;  // rows of `out` written (q < q_write)
+};
+
+// Build the contraction of a mode-n MTTKRP of tensor t.
+Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors, int mode);
+
+// Launch an MTTKRP-shaped contraction (FP32 or BF16 storage) on `stream`; out is
+// row-major [q_write][R].
+int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
+                       cudaStream_t stream);
+
+// Statistics helpers: count kernel launches; bracket a contraction with events.
+inline void count_launches(ptg_ctx *ctx, int n) { ctx->stats.launches += n; }
+int stats_begin(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t *ev);
+int stats_end(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t ev, double bytes, double flops);
+int stats_resolve(ptg_ctx *ctx);   // fold completed event pairs into the sums
+
+// ----------------------------------------------------------------------------------
+// Solver kernels (ptg_solve.cu)
+// ----------------------------------------------------------------------------------
+constexpr int kMaxInner = 50;  // include/NesterovMNLS.hpp:187
+
+// Device-side scalars of one NNLS solve, written by the FP64 eigen kernel.
+struct NnlsParams {
+  double Z[64 * 64];   // Hadamard of the Grams (FP64), R x R row-major
+  double L, mu, lambda, q;
+  float beta[kMaxInner];
+  int status;
+};
+
+int launch_eigen_bounds(const float *const *grams, int order, int mode, int R, NnlsParams *out,
+                        cudaStream_t stream);
+// Nesterov MNLS of one factor on a thread-block cluster; also writes the new Gram
+// (FP32 R x R), <M, A_new> and sum(Z .* G_new) in FP64, the iteration count and whether
+// the zero-column repair ran.
+int launch_nnls_full(ptg_ctx *ctx, const float *M, float *A, int I, int R, const NnlsParams *np,
+                     float delta1, float delta2, float *gram_out, double *inner_MA, double *had_ZG,
+                     int *iters_out, int *repaired_out, cudaStream_t stream);
+size_t gram_scratch_floats(int I, int R);
+int launch_gram(const float *A, int I, int R, float *G, float *part, cudaStream_t stream);
+int launch_normalize(float *const *fac, float *const *gram, const int *rows, int order, int weight,
+                     int R, cudaStream_t stream);
+int launch_accel_combine(const float *const *cur, const float *const *old, float *const *acc,
+                         const int *rows, int order, int R, double step, cudaStream_t stream);
+// out2[0] = <M, A_last> (FP64), out2[1] = sum(Z_last .* G_last) with Z_last the Hadamard
+// of grams[0..order-2].
+int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const float *const *grams,
+                      int order, int R, double *out2, cudaStream_t stream);
+
+}  // namespace ptg

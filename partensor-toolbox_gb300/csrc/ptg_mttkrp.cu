@@ -1,0 +1,475 @@
+// Dense MTTKRP on CUDA cores (FP32 math; FP32 or BF16 tensor storage).
+//
+// Replaces the reference's MTTKRP family: the sequential X_(n) * PartialKhatriRao
+// (include/MTTKRP.hpp:60-69), the blocked OpenMP version (include/MTTKRP.hpp:102-225)
+// and the cuBLAS-DGEMM-per-block hybrid (include/CUDA/CUDAMTTKRP.hpp:67-200).
+//
+// The tensor is read once, in its natural ColMajor order, viewed as [P, Q, S] with
+// Q the mode being solved.  No matricisation and no Khatri-Rao matrix are materialised:
+// each CTA forms the BK x R Khatri-Rao tile of its K-slice in shared memory from factor
+// rows.  The contraction is split over K across CTAs; every split writes its partial
+// Q x R block to scratch and a second kernel sums the splits in a fixed order, so the
+// result is bit-identical from run to run.
+#include <algorithm>
+#include <cstdio>
+
+#include "ptg_internal.h"
+
+namespace ptg {
+
+namespace {
+
+struct KrDev {  // kernel-parameter copy of a KrSide
+  int n;
+  uint32_t ext[PTG_MAX_ORDER];
+  uint32_t valid[PTG_MAX_ORDER];
+  const float *fac[PTG_MAX_ORDER];
+};
+
+struct SimtParams {
+  const void *X;
+  int64_t P, Q, S;
+  int64_t ktiles_total, ktiles_per_split, pblocks;
+  KrDev before, after;
+  int R, col0;       // factor row stride and first column handled by this launch
+  float *partial;    // [nsplit][Q][ldp] (ldp = BN)
+  float *out;        // used when nsplit == 1: row-major [q_write][ldo]
+  int64_t q_write;
+  int ldo;
+  int nsplit;
+};
+
+template <typename T>
+struct Vec;  // 16-byte global load unit
+template <>
+struct Vec<float> {
+  static constexpr int kElems = 4;
+};
+template <>
+struct Vec<__nv_bfloat16> {
+  static constexpr int kElems = 8;
+};
+
+__device__ __forceinline__ void unpack16(const uint4 &u, float *f, const float *) {
+  f[0] = __uint_as_float(u.x);
+  f[1] = __uint_as_float(u.y);
+  f[2] = __uint_as_float(u.z);
+  f[3] = __uint_as_float(u.w);
+}
+__device__ __forceinline__ void unpack16(const uint4 &u, float *f, const __nv_bfloat16 *) {
+  const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    f[2 * i] = __uint_as_float(w[i] << 16);
+    f[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+  }
+}
+
+// Khatri-Rao value of one side for linear index `lin` and NV consecutive columns.
+template <int NV>
+__device__ __forceinline__ void kr_side(const KrDev &s, uint32_t lin, int R, int c, float *v) {
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j] = 1.0f;
+  for (int f = 0; f < s.n; ++f) {
+    const uint32_t e = s.ext[f];
+    const uint32_t d = lin % e;
+    lin /= e;
+    if (d >= s.valid[f]) {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) v[j] = 0.0f;
+      return;
+    }
+    const float *row = s.fac[f] + (size_t)d * R;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] *= (c + j < R) ? __ldg(row + c + j) : 0.0f;
+  }
+}
+
+// Tile configuration: BN columns per launch, BM rows of Q, BK contraction elements.
+template <int BN>
+struct Cfg;
+template <>
+struct Cfg<16> {
+  static constexpr int TN = 4, TM = 4, BM = 128;
+};
+template <>
+struct Cfg<32> {
+  static constexpr int TN = 4, TM = 8, BM = 128;
+};
+template <>
+struct Cfg<64> {
+  static constexpr int TN = 8, TM = 8, BM = 128;
+};
+template <>
+struct Cfg<128> {
+  static constexpr int TN = 8, TM = 8, BM = 64;
+};
+
+constexpr int kThreads = 128;
+constexpr int BK = 32;
+
+// MMAJOR: mode-0 style (P == 1): q contiguous; tile [BK s][BM q]  -> Xs[k][m]
+// KMAJOR: P > 1: p contiguous within (q, s); tile [BM q][BK p]   -> Xs[m][k]
+template <typename T, int BN, bool MMAJOR>
+__global__ void __launch_bounds__(kThreads) mttkrp_simt_kernel(const SimtParams prm) {
+  using C = Cfg<BN>;
+  constexpr int BM = C::BM, TM = C::TM, TN = C::TN;
+  constexpr int NG = BN / TN;  // column groups
+  static_assert(NG * (BM / TM) == kThreads, "thread tiling");
+  constexpr int EV = Vec<T>::kElems;                   // elements per 16-byte load
+  constexpr int XLD = MMAJOR ? (BM + 4) : (BK + 4);    // smem row stride (floats)
+  constexpr int XROWS = MMAJOR ? BK : BM;
+  constexpr int LOADS = (BM * BK) / (EV * kThreads);   // 16-byte loads per thread per tile
+  static_assert(LOADS * EV * kThreads == BM * BK, "load tiling");
+
+  // dynamic shared memory: two X tiles then two Khatri-Rao tiles
+  extern __shared__ __align__(16) float smem_dyn[];
+  constexpr int XS = XROWS * XLD, KS = BK * BN;
+
+  const int tid = threadIdx.x;
+  const int ng = tid % NG, mg = tid / NG;
+  const int64_t q0 = (int64_t)blockIdx.x * BM;
+  const int split = blockIdx.y;
+  const int64_t t_begin = (int64_t)split * prm.ktiles_per_split;
+  const int64_t t_end = min(prm.ktiles_total, t_begin + prm.ktiles_per_split);
+  const T *X = reinterpret_cast<const T *>(prm.X);
+
+  float acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = 0.0f;
+
+  uint4 regs[LOADS];
+
+  // ---- global -> registers for tile t ----
+  auto load_tile = [&](int64_t t) {
+    if (MMAJOR) {
+      const int64_t s0 = t * BK;
+#pragma unroll
+      for (int i = 0; i < LOADS; ++i) {
+        const int f = tid + i * kThreads;
+        const int k = f / (BM / EV), mv = (f % (BM / EV)) * EV;
+        const int64_t s = s0 + k, q = q0 + mv;
+        if (s < prm.S && q < prm.Q)
+          regs[i] = __ldg(reinterpret_cast<const uint4 *>(X + q + prm.Q * s));
+        else
+          regs[i] = make_uint4(0, 0, 0, 0);
+      }
+    } else {
+      const int64_t s = t / prm.pblocks;
+      const int64_t p0 = (t % prm.pblocks) * BK;
+#pragma unroll
+      for (int i = 0; i < LOADS; ++i) {
+        const int f = tid + i * kThreads;
+        const int m = f / (BK / EV), kv = (f % (BK / EV)) * EV;
+        const int64_t p = p0 + kv, q = q0 + m;
+        if (p < prm.P && q < prm.Q)
+          regs[i] = __ldg(reinterpret_cast<const uint4 *>(X + p + prm.P * (q + prm.Q * s)));
+        else
+          regs[i] = make_uint4(0, 0, 0, 0);
+      }
+    }
+  };
+
+  // ---- registers -> shared, and the Khatri-Rao tile ----
+  auto store_tile = [&](int64_t t, int buf) {
+#pragma unroll
+    for (int i = 0; i < LOADS; ++i) {
+      const int f = tid + i * kThreads;
+      float v[EV];
+      unpack16(regs[i], v, (const T *)nullptr);
+      float *dst;
+      if (MMAJOR) {
+        const int k = f / (BM / EV), mv = (f % (BM / EV)) * EV;
+        dst = &smem_dyn[buf * XS + k * XLD + mv];
+      } else {
+        const int m = f / (BK / EV), kv = (f % (BK / EV)) * EV;
+        dst = &smem_dyn[buf * XS + m * XLD + kv];
+      }
+#pragma unroll
+      for (int e = 0; e < EV; e += 4)
+        *reinterpret_cast<float4 *>(dst + e) = make_float4(v[e], v[e + 1], v[e + 2], v[e + 3]);
+    }
+    // KR tile: thread -> one k row, KPT consecutive columns
+    constexpr int KPT = (BK * BN) / kThreads;
+    const int k = tid / (BN / KPT), c = (tid % (BN / KPT)) * KPT;
+    float va[KPT], vb[KPT];
+    if (MMAJOR) {
+      const int64_t s = t * BK + k;
+      if (s < prm.S) {
+        kr_side<KPT>(prm.after, (uint32_t)s, prm.R, prm.col0 + c, va);
+      } else {
+#pragma unroll
+        for (int j = 0; j < KPT; ++j) va[j] = 0.0f;
+      }
+#pragma unroll
+      for (int j = 0; j < KPT; ++j) vb[j] = 1.0f;
+    } else {
+      const int64_t s = t / prm.pblocks;
+      const int64_t p = (t % prm.pblocks) * BK + k;
+      kr_side<KPT>(prm.after, (uint32_t)s, prm.R, prm.col0 + c, va);
+      if (p < prm.P) {
+        kr_side<KPT>(prm.before, (uint32_t)p, prm.R, prm.col0 + c, vb);
+      } else {
+#pragma unroll
+        for (int j = 0; j < KPT; ++j) vb[j] = 0.0f;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < KPT; j += 4)
+      *reinterpret_cast<float4 *>(&smem_dyn[2 * XS + buf * KS + k * BN + c + j]) =
+          make_float4(va[j] * vb[j], va[j + 1] * vb[j + 1], va[j + 2] * vb[j + 2],
+                      va[j + 3] * vb[j + 3]);
+  };
+
+  auto compute = [&](int buf) {
+    const float *xs = smem_dyn + buf * XS;
+    const float *ks = smem_dyn + 2 * XS + buf * KS;
+    if (MMAJOR) {
+#pragma unroll 4
+      for (int k = 0; k < BK; ++k) {
+        float a[TM], b[TN];
+#pragma unroll
+        for (int i = 0; i < TM; i += 4) {
+          const float4 v = *reinterpret_cast<const float4 *>(xs + k * XLD + mg * TM + i);
+          a[i] = v.x; a[i + 1] = v.y; a[i + 2] = v.z; a[i + 3] = v.w;
+        }
+#pragma unroll
+        for (int j = 0; j < TN; j += 4) {
+          const float4 v = *reinterpret_cast<const float4 *>(ks + k * BN + ng * TN + j);
+          b[j] = v.x; b[j + 1] = v.y; b[j + 2] = v.z; b[j + 3] = v.w;
+        }
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+          for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+      }
+    } else {
+#pragma unroll 2
+      for (int k = 0; k < BK; k += 4) {
+        float a[TM][4], b[4][TN];
+#pragma unroll
+        for (int i = 0; i < TM; ++i) {
+          const float4 v = *reinterpret_cast<const float4 *>(xs + (mg + i * (BM / TM)) * XLD + k);
+          a[i][0] = v.x; a[i][1] = v.y; a[i][2] = v.z; a[i][3] = v.w;
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+          for (int j = 0; j < TN; j += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(ks + (k + kk) * BN + ng * TN + j);
+            b[kk][j] = v.x; b[kk][j + 1] = v.y; b[kk][j + 2] = v.z; b[kk][j + 3] = v.w;
+          }
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+#pragma unroll
+          for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(a[i][kk], b[kk][j], acc[i][j]);
+      }
+    }
+  };
+
+  if (t_begin < t_end) {
+    load_tile(t_begin);
+    store_tile(t_begin, 0);
+    __syncthreads();
+    int cur = 0;
+    for (int64_t t = t_begin; t < t_end; ++t) {
+      const bool more = (t + 1 < t_end);
+      if (more) load_tile(t + 1);
+      compute(cur);
+      if (more) store_tile(t + 1, cur ^ 1);
+      __syncthreads();
+      cur ^= 1;
+    }
+  }
+
+  // ---- epilogue: rows of this thread ----
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int m = MMAJOR ? (mg * TM + i) : (mg + i * (BM / TM));
+    const int64_t q = q0 + m;
+    if (q >= prm.Q) continue;
+    const int c = ng * TN;
+    if (prm.nsplit == 1) {
+      if (q < prm.q_write) {
+#pragma unroll
+        for (int j = 0; j < TN; ++j)
+          if (prm.col0 + c + j < prm.R) prm.out[q * prm.ldo + prm.col0 + c + j] = acc[i][j];
+      }
+    } else {
+      float *dst = prm.partial + ((int64_t)split * prm.Q + q) * BN + c;
+#pragma unroll
+      for (int j = 0; j < TN; j += 4)
+        *reinterpret_cast<float4 *>(dst + j) =
+            make_float4(acc[i][j], acc[i][j + 1], acc[i][j + 2], acc[i][j + 3]);
+    }
+  }
+}
+
+// out[q, col0 + c] = sum over splits of partial[split][q][c], in split order.
+__global__ void splitk_reduce_kernel(const float *__restrict__ partial, int nsplit, int64_t Q,
+                                     int BN, int64_t q_write, int R, int col0, int ldo,
+                                     float *__restrict__ out) {
+  const int64_t n = q_write * BN;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = idx / BN;
+    const int c = (int)(idx % BN);
+    if (col0 + c >= R) continue;
+    float s = 0.0f;
+    for (int sp = 0; sp < nsplit; ++sp) s += partial[((int64_t)sp * Q + q) * BN + c];
+    out[q * ldo + col0 + c] = s;
+  }
+}
+
+KrDev to_dev(const KrSide &s) {
+  KrDev d{};
+  d.n = s.n;
+  for (int i = 0; i < s.n; ++i) {
+    d.ext[i] = (uint32_t)s.ext[i];
+    d.valid[i] = (uint32_t)s.valid[i];
+    d.fac[i] = s.fac[i];
+  }
+  return d;
+}
+
+template <int BN>
+size_t simt_smem_bytes(bool mmajor) {
+  using Cf = Cfg<BN>;
+  const size_t xrows = mmajor ? BK : Cf::BM, xld = mmajor ? (Cf::BM + 4) : (BK + 4);
+  return sizeof(float) * (2 * xrows * xld + 2 * BK * BN);
+}
+
+template <typename T, int BN>
+int launch_cfg(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, int col0,
+               float *out, cudaStream_t stream) {
+  using Cf = Cfg<BN>;
+  const bool mmajor = (c.P == 1);
+  SimtParams prm{};
+  prm.X = t->data;
+  prm.P = c.P;
+  prm.Q = c.Q;
+  prm.S = c.S;
+  prm.before = to_dev(c.before);
+  prm.after = to_dev(c.after);
+  prm.R = R;
+  prm.col0 = col0;
+  prm.out = out;
+  prm.q_write = c.q_write;
+  prm.ldo = R;
+  if (mmajor) {
+    prm.pblocks = 1;
+    prm.ktiles_total = (c.S + BK - 1) / BK;
+  } else {
+    prm.pblocks = (c.P + BK - 1) / BK;
+    prm.ktiles_total = c.S * prm.pblocks;
+  }
+  const int64_t mtiles = (c.Q + Cf::BM - 1) / Cf::BM;
+  const int64_t target = (int64_t)ctx->sm_count * 4;
+  int64_t nsplit = std::max<int64_t>(1, (target + mtiles - 1) / mtiles);
+  nsplit = std::min<int64_t>(nsplit, prm.ktiles_total);
+  nsplit = std::max<int64_t>(nsplit, 1);
+  prm.ktiles_per_split = (prm.ktiles_total + nsplit - 1) / nsplit;
+  nsplit = (prm.ktiles_total + prm.ktiles_per_split - 1) / prm.ktiles_per_split;
+  prm.nsplit = (int)nsplit;
+  if (nsplit > 1) {
+    PTG_TRY(ctx->scratch.ensure((size_t)nsplit * c.Q * BN * sizeof(float)));
+    prm.partial = reinterpret_cast<float *>(ctx->scratch.ptr);
+  }
+  dim3 grid((unsigned)mtiles, (unsigned)nsplit);
+  const size_t smem = simt_smem_bytes<BN>(mmajor);
+  if (mmajor) {
+    PTG_CUDA(cudaFuncSetAttribute(mttkrp_simt_kernel<T, BN, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    mttkrp_simt_kernel<T, BN, true><<<grid, kThreads, smem, stream>>>(prm);
+  } else {
+    PTG_CUDA(cudaFuncSetAttribute(mttkrp_simt_kernel<T, BN, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    mttkrp_simt_kernel<T, BN, false><<<grid, kThreads, smem, stream>>>(prm);
+  }
+  PTG_CUDA(cudaGetLastError());
+  count_launches(ctx, nsplit > 1 ? 2 : 1);
+  if (nsplit > 1) {
+    const int64_t n = c.q_write * BN;
+    const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->sm_count * 8);
+    splitk_reduce_kernel<<<std::max(blocks, 1), 256, 0, stream>>>(
+        prm.partial, (int)nsplit, c.Q, BN, c.q_write, R, col0, R, out);
+    PTG_CUDA(cudaGetLastError());
+  }
+  return PTG_OK;
+}
+
+template <typename T>
+int launch_typed(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
+                 cudaStream_t stream) {
+  if (R <= 16) return launch_cfg<T, 16>(ctx, t, c, R, 0, out, stream);
+  if (R <= 32) return launch_cfg<T, 32>(ctx, t, c, R, 0, out, stream);
+  if (R <= 64) return launch_cfg<T, 64>(ctx, t, c, R, 0, out, stream);
+  // wider ranks: 128-column chunks (each chunk re-reads the tensor)
+  for (int c0 = 0; c0 < R; c0 += 128) PTG_TRY(launch_cfg<T, 128>(ctx, t, c, R, c0, out, stream));
+  return PTG_OK;
+}
+
+}  // namespace
+
+Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors, int mode) {
+  Contraction c;
+  const int N = t->order;
+  auto ext = [&](int k) { return k == 0 ? t->pdim0 : t->dims[k]; };
+  for (int k = 0; k < mode; ++k) {
+    c.P *= ext(k);
+    c.before.ext[c.before.n] = ext(k);
+    c.before.valid[c.before.n] = t->dims[k];
+    c.before.fac[c.before.n] = factors[k];
+    c.before.n++;
+  }
+  c.Q = ext(mode);
+  for (int k = mode + 1; k < N; ++k) {
+    c.S *= ext(k);
+    c.after.ext[c.after.n] = ext(k);
+    c.after.valid[c.after.n] = t->dims[k];
+    c.after.fac[c.after.n] = factors[k];
+    c.after.n++;
+  }
+  c.q_write = t->dims[mode];
+  return c;
+}
+
+// Algorithmic bytes of one contraction: the tensor entries (unpadded) in their storage
+// type, every factor row the Khatri-Rao tiles read, the FP32 result.
+static double contraction_bytes(const ptg_tensor *t, const Contraction &c, int R) {
+  double numel = 1.0;
+  for (int k = 0; k < t->order; ++k) numel *= (double)t->dims[k];
+  const double esz = t->dtype == PTG_F32 ? 4.0 : 2.0;
+  double fac = 0.0;
+  for (int i = 0; i < c.before.n; ++i) fac += (double)c.before.valid[i] * R * 4.0;
+  for (int i = 0; i < c.after.n; ++i) fac += (double)c.after.valid[i] * R * 4.0;
+  return numel * esz + fac + (double)c.q_write * R * 4.0;
+}
+
+int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
+                       cudaStream_t stream) {
+  if (R < 1) return set_error(PTG_ERR_INVALID, "rank must be >= 1");
+  if (c.P > 0xffffffffLL || c.S > 0xffffffffLL)
+    return set_error(PTG_ERR_UNSUPPORTED, "contraction extent exceeds 2^32");
+  if (c.P > 1 && (c.P % 8) != 0)
+    return set_error(PTG_ERR_INVALID, "internal: P must be a multiple of 8");
+  cudaEvent_t ev = nullptr;
+  PTG_TRY(stats_begin(ctx, stream, &ev));
+  int rc;
+  if (t->dtype == PTG_F32)
+    rc = launch_typed<float>(ctx, t, c, R, out, stream);
+  else if (t->dtype == PTG_BF16)
+    rc = launch_typed<__nv_bfloat16>(ctx, t, c, R, out, stream);
+  else
+    return set_error(PTG_ERR_UNSUPPORTED, "tensor dtype");
+  if (rc != PTG_OK) return rc;
+  double numel = 1.0;
+  for (int k = 0; k < t->order; ++k) numel *= (double)t->dims[k];
+  return stats_end(ctx, stream, ev, contraction_bytes(t, c, R), 2.0 * numel * R);
+}
+
+}  // namespace ptg

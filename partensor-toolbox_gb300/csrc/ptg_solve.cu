@@ -1,0 +1,756 @@
+// Per-mode solver kernels of the CPD-ALS sweep.
+//
+//   eigen_bounds_kernel  FP64: Z = Hadamard of the Grams (include/PartialCwiseProd.hpp:54-222),
+//                        its extreme eigenvalues (= singular values of the SPD Z,
+//                        include/NesterovMNLS.hpp:45-52), GLambda (:75-91) and the beta
+//                        sequence of UpdateAlpha (:103-113, :224-226).
+//   nnls_cluster_kernel  the dense Nesterov MNLS (include/NesterovMNLS.hpp:181-234) over all
+//                        rows of a factor on one thread-block cluster, with the global KKT
+//                        stop test reduced through distributed shared memory, followed by the
+//                        zero-column repair (include/Cpd.hpp:206-207), the Gram A^T A
+//                        (include/Cpd.hpp:227) and the FP64 cost term <M, A>.
+//   normalize_kernel     include/Normalize.hpp:92-174 (quirks included).
+//   accel_combine_kernel A_acc = A_old + s (A - A_old)  (include/Cpd.hpp:257-261).
+//   gram / cost-term kernels.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+
+#include "ptg_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace ptg {
+
+namespace {
+
+// ------------------------------------------------------------------------------------
+// FP64 eigenvalue bounds.  Householder reduction to tridiagonal form (Householder 1958;
+// Golub & Van Loan, Matrix Computations, alg. 8.3.1) and Sturm-sequence bisection
+// (Givens 1954; Wilkinson, The Algebraic Eigenvalue Problem, ch. 5) run as a 128-way
+// multisection per round.
+// ------------------------------------------------------------------------------------
+constexpr int kEigThreads = 256;
+constexpr int kMaxR = 64;
+
+struct GramPtrs {
+  const float *g[PTG_MAX_ORDER];
+};
+
+__device__ int sturm_count(const double *d, const double *e2, int n, double x) {
+  int cnt = 0;
+  double q = d[0] - x;
+  if (q < 0.0) ++cnt;
+  for (int i = 1; i < n; ++i) {
+    if (q == 0.0) q = 1e-300;
+    q = (d[i] - x) - e2[i - 1] / q;
+    if (q < 0.0) ++cnt;
+  }
+  return cnt;
+}
+
+__global__ void __launch_bounds__(kEigThreads)
+eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
+  __shared__ double A[kMaxR * kMaxR];
+  __shared__ double v[kMaxR], p[kMaxR], w[kMaxR];
+  __shared__ double d[kMaxR], e[kMaxR], e2[kMaxR];
+  __shared__ double red[kEigThreads / 32];
+  __shared__ double s_scalar[4];
+  __shared__ double lohi[2][2];
+  __shared__ int firsthit[2];
+  const int tid = threadIdx.x;
+  const int n = R;
+
+  // Z = prod_{k != mode} G_k (FP64), k from order-1 down to 0 as PartialCwiseProd orders it
+  for (int idx = tid; idx < n * n; idx += blockDim.x) {
+    double z = 1.0;
+    for (int k = order - 1; k >= 0; --k)
+      if (k != mode) z *= (double)gp.g[k][idx];
+    A[idx] = z;
+    out->Z[idx] = z;
+  }
+  __syncthreads();
+
+  auto block_sum = [&](double x) -> double {
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((tid & 31) == 0) red[tid >> 5] = x;
+    __syncthreads();
+    double s = 0.0;
+    for (int i = 0; i < kEigThreads / 32; ++i) s += red[i];
+    __syncthreads();
+    return s;
+  };
+
+  // ---- Householder tridiagonalisation (A symmetric, row-major n x n) ----
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m = n - k - 1;  // length of the column below the diagonal
+    // sigma = ||x[1:]||^2
+    double part = 0.0;
+    for (int i = 1 + tid; i < m; i += blockDim.x) {
+      const double xi = A[(k + 1 + i) * n + k];
+      part += xi * xi;
+    }
+    const double sigma = block_sum(part);
+    const double x0 = A[(k + 1) * n + k];
+    if (sigma == 0.0) {
+      if (tid == 0) e[k] = x0;
+      __syncthreads();
+      continue;
+    }
+    const double alpha = (x0 >= 0.0 ? -1.0 : 1.0) * sqrt(x0 * x0 + sigma);
+    for (int i = tid; i < m; i += blockDim.x) v[i] = (i == 0) ? (x0 - alpha) : A[(k + 1 + i) * n + k];
+    __syncthreads();
+    const double vtv = (x0 - alpha) * (x0 - alpha) + sigma;
+    const double beta = 2.0 / vtv;
+    // p = beta * A_sub v   (rows of the trailing block split over the threads)
+    for (int i = tid; i < m; i += blockDim.x) {
+      const double *row = &A[(k + 1 + i) * n + (k + 1)];
+      double s = 0.0;
+      for (int j = 0; j < m; ++j) s = fma(row[j], v[j], s);
+      p[i] = beta * s;
+    }
+    __syncthreads();
+    part = 0.0;
+    for (int i = tid; i < m; i += blockDim.x) part = fma(p[i], v[i], part);
+    const double K = 0.5 * beta * block_sum(part);
+    for (int i = tid; i < m; i += blockDim.x) w[i] = p[i] - K * v[i];
+    __syncthreads();
+    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+      const int i = idx / m, j = idx % m;
+      A[(k + 1 + i) * n + (k + 1 + j)] -= v[i] * w[j] + w[i] * v[j];
+    }
+    if (tid == 0) e[k] = alpha;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    for (int i = 0; i < n; ++i) d[i] = A[i * n + i];
+    if (n >= 2) e[n - 2] = A[(n - 1) * n + (n - 2)];
+    for (int i = 0; i + 1 < n; ++i) e2[i] = e[i] * e[i];
+    // Gershgorin interval
+    double lo = 1e300, hi = -1e300;
+    for (int i = 0; i < n; ++i) {
+      const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
+      lo = fmin(lo, d[i] - r);
+      hi = fmax(hi, d[i] + r);
+    }
+    const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
+    lo -= pad;
+    hi += pad;
+    lohi[0][0] = lo; lohi[0][1] = hi;   // smallest eigenvalue
+    lohi[1][0] = lo; lohi[1][1] = hi;   // largest eigenvalue
+  }
+  __syncthreads();
+
+  // ---- multisection: threads 0..127 bracket the smallest, 128..255 the largest ----
+  const int which = tid >> 7;      // 0: min, 1: max
+  const int j = tid & 127;
+  const int target = which == 0 ? 1 : n;  // count(x) >= target  <=>  x > lambda
+  for (int round = 0; round < 12; ++round) {
+    const double lo = lohi[which][0], hi = lohi[which][1];
+    const double x = lo + (hi - lo) * (double)(j + 1) / 129.0;
+    const int hit = sturm_count(d, e2, n, x) >= target;
+    if (j == 0) firsthit[which] = 128;
+    __syncthreads();
+    if (hit) atomicMin(&firsthit[which], j);
+    __syncthreads();
+    if (j == 0) {
+      const int f = firsthit[which];
+      const double nlo = (f == 0) ? lo : lo + (hi - lo) * (double)f / 129.0;
+      const double nhi = (f == 128) ? hi : lo + (hi - lo) * (double)(f + 1) / 129.0;
+      lohi[which][0] = nlo;
+      lohi[which][1] = nhi;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const double lmin = 0.5 * (lohi[0][0] + lohi[0][1]);
+    const double lmax = 0.5 * (lohi[1][0] + lohi[1][1]);
+    // singular values of a symmetric matrix are |eigenvalues|
+    double L = fmax(fabs(lmax), fabs(lmin));
+    double mu = fabs(lmin);
+    if (n == 1) L = mu = fabs(d[0]);
+    // GLambda, include/NesterovMNLS.hpp:75-91
+    double q = mu / L, lam;
+    if (1.0 / q > 1e6) lam = 10.0 * mu;
+    else if (1.0 / q > 1e3) lam = mu;
+    else lam = mu / 10.0;
+    L += lam;
+    mu += lam;
+    q = mu / L;
+    out->L = L;
+    out->mu = mu;
+    out->lambda = lam;
+    out->q = q;
+    double alpha = 1.0;
+    for (int it = 0; it < kMaxInner; ++it) {   // UpdateAlpha, :103-113
+      const double b = alpha * alpha - q, c = -alpha * alpha;
+      const double na = (-b + sqrt(b * b - 4.0 * c)) / 2.0;
+      out->beta[it] = (float)(alpha * (1.0 - alpha) / (alpha * alpha + na));
+      alpha = na;
+    }
+    out->status = (isfinite(L) && isfinite(mu)) ? 0 : PTG_ERR_NUMERIC;
+    s_scalar[0] = L;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Row-batched Nesterov MNLS on one cluster.
+// ------------------------------------------------------------------------------------
+constexpr int kNnlsWarps = 16;
+constexpr int kNnlsThreads = kNnlsWarps * 32;
+
+struct NnlsArgs {
+  const float *M;        // [I][R]
+  float *A;              // [I][R] in: prox centre / start, out: solution
+  int I, R;
+  const NnlsParams *np;
+  float delta1, delta2;
+  float *gram_out;       // [R][R]
+  double *inner_MA;      // <M, A_new> (FP64)
+  double *had_ZG;        // sum(Z .* G_new) (FP64)
+  int *iters_out;
+  int *repaired_out;
+};
+
+template <int RB, int ROWS>
+__global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const NnlsArgs a) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CS = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int R = a.R, I = a.I;
+
+  extern __shared__ __align__(16) float sm[];
+  float *Zt = sm;                                   // R*R
+  float *As = Zt + R * R;                           // (kNnlsWarps*ROWS) x R
+  float *Gp = As + kNnlsWarps * ROWS * R;           // R*R  (this CTA's partial Gram)
+  float *colsum = Gp + R * R;                       // R
+  double *slots = reinterpret_cast<double *>(colsum + ((R + 1) & ~1));  // [2][2] stop test
+  double *wred = slots + 4;                         // kNnlsWarps * 2
+  double *ma = wred + 2 * kNnlsWarps;               // 1: this CTA's <M, A>
+  int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired
+
+  const NnlsParams *np = a.np;
+  const float L = (float)np->L, lam = (float)np->lambda;
+  const float invL = 1.0f / L;
+  for (int idx = tid; idx < R * R; idx += blockDim.x) {
+    float z = (float)np->Z[idx];
+    if (idx / R == idx % R) z += lam;               // Z~ = Z + lambda I   (:205)
+    Zt[idx] = z;
+  }
+
+  // rows of this lane: row(j) = gw + j * (CS * warps)
+  const int gw = rank * kNnlsWarps + warp;
+  const int stride = CS * kNnlsWarps;
+  float Y[ROWS][RB], Ac[ROWS][RB], Wt[ROWS][RB];
+  bool colok[RB];
+#pragma unroll
+  for (int b = 0; b < RB; ++b) colok[b] = (lane + 32 * b) < R;
+#pragma unroll
+  for (int j = 0; j < ROWS; ++j) {
+    const int i = gw + j * stride;
+#pragma unroll
+    for (int b = 0; b < RB; ++b) {
+      const int c = lane + 32 * b;
+      float a0 = 0.f, m = 0.f;
+      if (i < I && colok[b]) {
+        a0 = a.A[(size_t)i * R + c];
+        m = a.M[(size_t)i * R + c];
+      }
+      Ac[j][b] = a0;
+      Y[j][b] = a0;
+      Wt[j][b] = m + lam * a0;                      // W~ = W + lambda A0   (:206)
+    }
+  }
+  __syncthreads();
+
+  int it = 0;
+  for (;;) {
+    // grad = Y Z~ - W~ ; stop-test partials
+    float g[ROWS][RB];
+    float mx = 0.0f, mn = INFINITY;
+#pragma unroll
+    for (int j = 0; j < ROWS; ++j)
+#pragma unroll
+      for (int b = 0; b < RB; ++b) g[j][b] = -Wt[j][b];
+    for (int k = 0; k < R; ++k) {
+      const int kb = k >> 5, kl = k & 31;
+      float z[RB];
+#pragma unroll
+      for (int b = 0; b < RB; ++b) z[b] = colok[b] ? Zt[k * R + lane + 32 * b] : 0.f;
+#pragma unroll
+      for (int j = 0; j < ROWS; ++j) {
+        const float yk = __shfl_sync(0xffffffffu, kb == 0 ? Y[j][0] : Y[j][RB - 1], kl);
+#pragma unroll
+        for (int b = 0; b < RB; ++b) g[j][b] = fmaf(yk, z[b], g[j][b]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < ROWS; ++j) {
+      const bool rowok = (gw + j * stride) < I;
+#pragma unroll
+      for (int b = 0; b < RB; ++b)
+        if (rowok && colok[b]) {
+          mx = fmaxf(mx, fabsf(g[j][b] * Y[j][b]));
+          mn = fminf(mn, g[j][b]);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+    }
+    if (lane == 0) {
+      wred[2 * warp] = mx;
+      wred[2 * warp + 1] = mn;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double M1 = 0.0, M2 = INFINITY;
+      for (int w = 0; w < kNnlsWarps; ++w) {
+        M1 = fmax(M1, wred[2 * w]);
+        M2 = fmin(M2, wred[2 * w + 1]);
+      }
+      slots[2 * (it & 1)] = M1;
+      slots[2 * (it & 1) + 1] = M2;
+    }
+    cluster.sync();
+    double gmx = 0.0, gmn = INFINITY;
+    if (lane < CS) {
+      const double *rs = cluster.map_shared_rank(slots, lane);
+      gmx = rs[2 * (it & 1)];
+      gmn = rs[2 * (it & 1) + 1];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      gmx = fmax(gmx, __shfl_xor_sync(0xffffffffu, gmx, o));
+      gmn = fmin(gmn, __shfl_xor_sync(0xffffffffu, gmn, o));
+    }
+    // stop test of include/NesterovMNLS.hpp:217-218
+    if ((gmx <= (double)a.delta1 && gmn >= -(double)a.delta2) || it >= kMaxInner) break;
+    const float beta = np->beta[it];
+#pragma unroll
+    for (int j = 0; j < ROWS; ++j)
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        const float na = fmaxf(Y[j][b] - g[j][b] * invL, 0.0f);       // :220
+        Y[j][b] = (1.0f + beta) * na - beta * Ac[j][b];                 // :228
+        Ac[j][b] = na;
+      }
+    ++it;
+  }
+
+  // ---- zero-column test (sum of |A| per column over all rows), include/Cpd.hpp:206 ----
+  for (int c = tid; c < R; c += blockDim.x) colsum[c] = 0.0f;
+  __syncthreads();
+  // per-warp column partials -> As as scratch, then fixed-order sum into colsum
+#pragma unroll
+  for (int b = 0; b < RB; ++b) {
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < ROWS; ++j) s += fabsf(Ac[j][b]);
+    if (colok[b]) As[warp * R + lane + 32 * b] = s;
+  }
+  __syncthreads();
+  for (int c = tid; c < R; c += blockDim.x) {
+    float s = 0.f;
+    for (int w = 0; w < kNnlsWarps; ++w) s += As[w * R + c];
+    colsum[c] = s;
+  }
+  cluster.sync();
+  if (tid == 0) {
+    float mincol = INFINITY;
+    for (int c = 0; c < R; ++c) {
+      float s = 0.f;
+      for (int r2 = 0; r2 < CS; ++r2) s += cluster.map_shared_rank(colsum, r2)[c];
+      mincol = fminf(mincol, s);
+    }
+    flags[0] = (mincol == 0.0f) ? 1 : 0;
+  }
+  __syncthreads();
+  const bool repair = flags[0] != 0;
+
+  // ---- final rows: repair, write A, stage rows for the Gram, <M, A> in FP64 ----
+  double ma_part = 0.0;
+#pragma unroll
+  for (int j = 0; j < ROWS; ++j) {
+    const int i = gw + j * stride;
+#pragma unroll
+    for (int b = 0; b < RB; ++b) {
+      const int c = lane + 32 * b;
+      float v = 0.f;
+      if (i < I && colok[b]) {
+        v = Ac[j][b];
+        if (repair) v = 0.9f * v + 0.1f * a.A[(size_t)i * R + c];   // :206-207
+      }
+      if (colok[b]) As[(warp * ROWS + j) * R + c] = v;
+      if (i < I && colok[b]) ma_part = fma((double)a.M[(size_t)i * R + c], (double)v, ma_part);
+    }
+  }
+  __syncthreads();   // every CTA has read its old A rows before anyone writes new ones
+  cluster.sync();
+#pragma unroll
+  for (int j = 0; j < ROWS; ++j) {
+    const int i = gw + j * stride;
+#pragma unroll
+    for (int b = 0; b < RB; ++b) {
+      const int c = lane + 32 * b;
+      if (i < I && colok[b]) a.A[(size_t)i * R + c] = As[(warp * ROWS + j) * R + c];
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) ma_part += __shfl_xor_sync(0xffffffffu, ma_part, o);
+  if (lane == 0) wred[warp] = ma_part;
+  // partial Gram of this CTA's rows
+  const int nrows = kNnlsWarps * ROWS;
+  for (int idx = tid; idx < R * R; idx += blockDim.x) {
+    const int r1 = idx / R, r2 = idx % R;
+    float s = 0.f;
+    for (int i = 0; i < nrows; ++i) s = fmaf(As[i * R + r1], As[i * R + r2], s);
+    Gp[idx] = s;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kNnlsWarps; ++w) s += wred[w];
+    ma[0] = s;
+  }
+  cluster.sync();
+  if (rank == 0) {
+    for (int idx = tid; idx < R * R; idx += blockDim.x) {
+      float s = 0.f;
+      for (int r2 = 0; r2 < CS; ++r2) s += cluster.map_shared_rank(Gp, r2)[idx];
+      a.gram_out[idx] = s;
+      Zt[idx] = s;   // reuse Zt (no longer needed) for the FP64 Hadamard sum
+    }
+    __syncthreads();
+    if (warp == 0) {
+      double h = 0.0;
+      for (int idx = lane; idx < R * R; idx += 32) h = fma(np->Z[idx], (double)Zt[idx], h);
+      for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+      if (lane == 0) {
+        double sma = 0.0;
+        for (int r2 = 0; r2 < CS; ++r2) sma += cluster.map_shared_rank(ma, r2)[0];
+        *a.inner_MA = sma;
+        *a.had_ZG = h;
+        *a.iters_out = it;
+        *a.repaired_out = repair ? 1 : 0;
+      }
+    }
+  }
+  cluster.sync();   // keep every CTA's shared memory alive until rank 0 has read it
+}
+
+template <int RB, int ROWS>
+size_t nnls_smem_bytes(int R) {
+  return sizeof(float) * (2 * R * R + kNnlsWarps * ROWS * R + ((R + 1) & ~1)) +
+         sizeof(double) * (4 + 2 * kNnlsWarps + 2) + 16;
+}
+
+template <int RB, int ROWS>
+int launch_nnls_t(int cs, const NnlsArgs &args, cudaStream_t stream) {
+  auto kern = nnls_cluster_kernel<RB, ROWS>;
+  const size_t smem = nnls_smem_bytes<RB, ROWS>(args.R);
+  PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (cs > 8) PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  if ((int64_t)cs * kNnlsWarps * ROWS < args.I)
+    return set_error(PTG_ERR_INVALID, "internal: NNLS row tiling");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cs, 1, 1);
+  cfg.blockDim = dim3(kNnlsThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PTG_CUDA(cudaLaunchKernelEx(&cfg, kern, args));
+  return PTG_OK;
+}
+
+// Cluster size of the NNLS kernel on this device: 16 (non-portable) when the hardware
+// can schedule it, else the portable 8.  Probed once per context.
+int nnls_cluster_size(ptg_ctx *ctx) {
+  if (ctx->nnls_cluster) return ctx->nnls_cluster;
+  int cs = 8;
+  auto kern = nnls_cluster_kernel<2, 16>;
+  const size_t smem = nnls_smem_bytes<2, 16>(kMaxR);
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess &&
+      cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16, 1, 1);
+    cfg.blockDim = dim3(kNnlsThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters > 0) cs = 16;
+  }
+  cudaGetLastError();
+  ctx->nnls_cluster = cs;
+  return cs;
+}
+
+// ------------------------------------------------------------------------------------
+// Gram, normalisation, acceleration, cost terms.
+// ------------------------------------------------------------------------------------
+constexpr int kGramRowsPerBlock = 256;
+
+__global__ void gram_partial_kernel(const float *__restrict__ A, int I, int R,
+                                    float *__restrict__ part) {
+  extern __shared__ float rows[];   // kGramRowsPerBlock x R
+  const int r0 = blockIdx.x * kGramRowsPerBlock;
+  const int nr = min(kGramRowsPerBlock, I - r0);
+  for (int idx = threadIdx.x; idx < nr * R; idx += blockDim.x) rows[idx] = A[(size_t)r0 * R + idx];
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
+    const int a = idx / R, b = idx % R;
+    float s = 0.f;
+    for (int i = 0; i < nr; ++i) s = fmaf(rows[i * R + a], rows[i * R + b], s);
+    part[(size_t)blockIdx.x * R * R + idx] = s;
+  }
+}
+
+__global__ void sum_rr_kernel(const float *__restrict__ part, int nb, int RR, float *__restrict__ G) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < RR; idx += gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int b = 0; b < nb; ++b) s += part[(size_t)b * RR + idx];
+    G[idx] = s;
+  }
+}
+
+}  // namespace
+
+int launch_eigen_bounds(const float *const *grams, int order, int mode, int R, NnlsParams *out,
+                        cudaStream_t stream) {
+  if (R > kMaxR) return set_error(PTG_ERR_UNSUPPORTED, "rank > 64 is not supported by the NNLS path");
+  GramPtrs gp{};
+  for (int k = 0; k < order; ++k) gp.g[k] = grams[k];
+  eigen_bounds_kernel<<<1, kEigThreads, 0, stream>>>(gp, order, mode, R, out);
+  PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
+}
+
+int launch_nnls_full(ptg_ctx *ctx, const float *M, float *A, int I, int R, const NnlsParams *np,
+                     float delta1, float delta2, float *gram_out, double *inner_MA, double *had_ZG,
+                     int *iters_out, int *repaired_out, cudaStream_t stream) {
+  if (R > kMaxR) return set_error(PTG_ERR_UNSUPPORTED, "rank > 64 is not supported by the NNLS path");
+  NnlsArgs args{M, A, I, R, np, delta1, delta2, gram_out, inner_MA, had_ZG, iters_out, repaired_out};
+  const int cs = nnls_cluster_size(ctx);
+  const int cap = cs * kNnlsWarps;   // rows per register slot
+  const int rows = (I + cap - 1) / cap;
+  const bool wide = R > 32;
+#define PTG_NNLS_CASE(RWS)                                                    \
+  if (rows <= RWS)                                                            \
+    return wide ? launch_nnls_t<2, RWS>(cs, args, stream)                     \
+                : launch_nnls_t<1, RWS>(cs, args, stream);
+  PTG_NNLS_CASE(1)
+  PTG_NNLS_CASE(2)
+  PTG_NNLS_CASE(4)
+  PTG_NNLS_CASE(8)
+  PTG_NNLS_CASE(16)
+#undef PTG_NNLS_CASE
+  return set_error(PTG_ERR_UNSUPPORTED, "factor has too many rows for the NNLS kernel");
+}
+
+int launch_gram(const float *A, int I, int R, float *G, float *part, cudaStream_t stream) {
+  const int nb = (I + kGramRowsPerBlock - 1) / kGramRowsPerBlock;
+  const size_t smem = sizeof(float) * kGramRowsPerBlock * R;
+  PTG_CUDA(cudaFuncSetAttribute(gram_partial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  gram_partial_kernel<<<nb, 256, smem, stream>>>(A, I, R, part);
+  sum_rr_kernel<<<(R * R + 255) / 256, 256, 0, stream>>>(part, nb, R * R, G);
+  PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
+}
+
+size_t gram_scratch_floats(int I, int R) {
+  return (size_t)((I + kGramRowsPerBlock - 1) / kGramRowsPerBlock) * R * R;
+}
+
+// ---- Normalize ----
+struct NormArgs {
+  float *fac[PTG_MAX_ORDER];
+  float *gram[PTG_MAX_ORDER];
+  int rows[PTG_MAX_ORDER];
+  int order, weight, R;
+};
+
+// Column multipliers of include/Normalize.hpp:92-174 for column c.
+__device__ void normalize_column(const NormArgs &a, int c, float *mult /*[order]*/, float *lf /*[order]*/) {
+  const int N = a.order, last = N - 1, w = a.weight;
+  // the factor behind lambda_fac[last-1] decides nonZeroFlag
+  const int flag_fac = (w <= N - 2) ? (N - 1) : (N - 2);
+  const bool nonzero = sqrtf(a.gram[flag_fac][c * a.R + c]) != 0.0f;
+  float cumul = 1.0f;
+  for (int k = 0; k < N; ++k) {
+    mult[k] = 1.0f;
+    lf[k] = 1.0f;
+  }
+  for (int j = 0; j < last; ++j) {
+    if (j == w) continue;
+    const float nf = sqrtf(a.gram[j][c * a.R + c]);
+    if (nonzero) {
+      mult[j] = 1.0f / nf;
+      cumul *= nf;
+      lf[j] = nf;
+    }
+  }
+  if (nonzero) mult[w] = cumul;
+}
+
+__global__ void normalize_factors_kernel(NormArgs a) {
+  // one thread per (factor row, column) element across all factors, then the Grams
+  extern __shared__ float sh[];   // mult[order][R], lf[order][R]
+  float *mult = sh, *lfs = sh + a.order * a.R;
+  for (int c = threadIdx.x; c < a.R; c += blockDim.x) {
+    float m[PTG_MAX_ORDER], l[PTG_MAX_ORDER];
+    normalize_column(a, c, m, l);
+    for (int k = 0; k < a.order; ++k) {
+      mult[k * a.R + c] = m[k];
+      lfs[k * a.R + c] = l[k];
+    }
+  }
+  __syncthreads();
+  // every block reads the Grams (diagonals) above; writes happen in a second kernel
+  for (int k = 0; k < a.order; ++k) {
+    const int64_t n = (int64_t)a.rows[k] * a.R;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (int64_t)gridDim.x * blockDim.x)
+      a.fac[k][idx] *= mult[k * a.R + (int)(idx % a.R)];
+  }
+}
+
+__global__ void normalize_grams_kernel(NormArgs a) {
+  // single block: Gram scaling G_j ./= lf lf^T, G_w .*= prod_j lf_j lf_j^T  (:159-172)
+  extern __shared__ float sh[];
+  float *lfs = sh;   // [order][R]
+  for (int c = threadIdx.x; c < a.R; c += blockDim.x) {
+    float m[PTG_MAX_ORDER], l[PTG_MAX_ORDER];
+    normalize_column(a, c, m, l);
+    for (int k = 0; k < a.order; ++k) lfs[k * a.R + c] = l[k];
+  }
+  __syncthreads();
+  const int N = a.order, last = N - 1, w = a.weight, R = a.R;
+  for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
+    const int r1 = idx / R, r2 = idx % R;
+    float wm = 1.0f;
+    for (int j = 0; j < last; ++j) {
+      if (j == w) continue;
+      const float nm = lfs[j * R + r1] * lfs[j * R + r2];
+      wm *= nm;
+      a.gram[j][idx] = a.gram[j][idx] / nm;
+    }
+    a.gram[w][idx] *= wm;
+  }
+}
+
+int launch_normalize(float *const *fac, float *const *gram, const int *rows, int order, int weight,
+                     int R, cudaStream_t stream) {
+  NormArgs a{};
+  for (int k = 0; k < order; ++k) {
+    a.fac[k] = fac[k];
+    a.gram[k] = gram[k];
+    a.rows[k] = rows[k];
+  }
+  a.order = order;
+  a.weight = weight;
+  a.R = R;
+  const size_t smem = sizeof(float) * 2 * order * R;
+  int64_t total = 0;
+  for (int k = 0; k < order; ++k) total += (int64_t)rows[k] * R;
+  const int blocks = (int)std::min<int64_t>(std::max<int64_t>(1, (total + 255) / 256), 1024);
+  // factors first (they read the unmodified Gram diagonals), then the Grams
+  normalize_factors_kernel<<<blocks, 256, smem, stream>>>(a);
+  normalize_grams_kernel<<<1, 256, smem, stream>>>(a);
+  PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
+}
+
+// ---- acceleration: acc = old + s (cur - old) for all factors ----
+struct AxpyArgs {
+  const float *cur[PTG_MAX_ORDER];
+  const float *old[PTG_MAX_ORDER];
+  float *acc[PTG_MAX_ORDER];
+  int64_t n[PTG_MAX_ORDER];
+  int order;
+  float step;
+};
+
+__global__ void accel_combine_kernel(AxpyArgs a) {
+  for (int k = 0; k < a.order; ++k)
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < a.n[k];
+         idx += (int64_t)gridDim.x * blockDim.x) {
+      const float o = a.old[k][idx];
+      a.acc[k][idx] = o + a.step * (a.cur[k][idx] - o);
+    }
+}
+
+int launch_accel_combine(const float *const *cur, const float *const *old, float *const *acc,
+                         const int *rows, int order, int R, double step, cudaStream_t stream) {
+  AxpyArgs a{};
+  int64_t total = 0;
+  for (int k = 0; k < order; ++k) {
+    a.cur[k] = cur[k];
+    a.old[k] = old[k];
+    a.acc[k] = acc[k];
+    a.n[k] = (int64_t)rows[k] * R;
+    total += a.n[k];
+  }
+  a.order = order;
+  a.step = (float)step;
+  const int blocks = (int)std::min<int64_t>(std::max<int64_t>(1, (total + 255) / 256), 1024);
+  accel_combine_kernel<<<blocks, 256, 0, stream>>>(a);
+  PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
+}
+
+// ---- FP64 cost terms for a given point: <M, A_last> and sum(Z .* G_last) ----
+__global__ void cost_terms_kernel(const float *__restrict__ M, const float *__restrict__ A, int64_t n,
+                                  GramPtrs gp, int order, int R, double *out2) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t idx = threadIdx.x; idx < n; idx += blockDim.x) s = fma((double)M[idx], (double)A[idx], s);
+  double h = 0.0;
+  for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
+    double z = 1.0;
+    for (int k = order - 2; k >= 0; --k) z *= (double)gp.g[k][idx];
+    h = fma(z, (double)gp.g[order - 1][idx], h);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, o);
+    h += __shfl_down_sync(0xffffffffu, h, o);
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[w] = s;
+    red[16 + w] = h;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+      a += red[i];
+      b += red[16 + i];
+    }
+    out2[0] = a;
+    out2[1] = b;
+  }
+}
+
+int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const float *const *grams,
+                      int order, int R, double *out2, cudaStream_t stream) {
+  GramPtrs gp{};
+  for (int k = 0; k < order; ++k) gp.g[k] = grams[k];
+  cost_terms_kernel<<<1, 512, 0, stream>>>(M, A_last, I_last * R, gp, order, R, out2);
+  PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
+}
+
+}  // namespace ptg
