@@ -1,0 +1,339 @@
+"""Headline benchmark: nonnegative CPD-ALS time to target fit on one GB300.
+
+Workload (the 1000^3 configuration): 3-way dense tensor 1000 x 1000 x 1000, rank R=32,
+ground-truth factors i.i.d. U[0,1] with column norms equalised (seed 2), 30 dB Gaussian
+noise, initial factors U[0,1] (seed 3), nonnegativity on every mode, reference defaults
+otherwise (Nesterov delta 1e-2, acceleration and normalisation on).  Synthetic data of
+that shape stands in for user data.
+
+A step is one full solve to the target: relative fit error <= noise floor + 1e-3, where the
+noise floor ||noise||/||X|| (computed in FP64 when the data is generated) is the error the
+FP64 least-squares optimum reaches up to O(R*sum(I)/prod(I)) = 1e-4 of overfit, so the
+target is "within 1e-3 of the FP64 oracle's converged fit".
+
+  value    BF16 tensor storage + tcgen05 MTTKRP + one FP32 refinement sweep, tensor already
+           resident in HBM (seconds per solve, lower is better)
+  plain    the same solve with FP32 storage and CUDA-core MTTKRP (reported beside it)
+  e2e      the one-call C ABI (ptg_cpd) from a pinned host FP64 buffer: host->device copy,
+           BF16 and FP32 conversion, solve, factor download, all inside the timed region
+  roofline MTTKRP launches timed live with CUDA events on their stream inside the timed
+           region; algorithmic bytes = prod(I)*2 + sum_{k != n} I_k*R*4 + I_n*R*4
+  cpu_baseline  the FP64 OpenMP restatement of the reference's CpdOpenMP (oracle/cpd_omp.c)
+           on the host cores, one full-size ALS sweep timed and scaled by the sweeps the FP64
+           algorithm needs (the FP32 plain form tracks the FP64 trajectory sweep by sweep)
+
+Inputs (2 GB BF16, 4 GB FP32) are far larger than the 129 MB L2, so no flush is needed
+between steps.  ``--impl reference`` times the CPU restatement alone.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIMS = [1000, 1000, 1000]
+RANK = 32
+SEED, INIT_SEED, SNR_DB = 2, 3, 30.0
+METRIC = "time to rel. fit err <= FP64-oracle fit + 1e-3 (BF16 tcgen05 MTTKRP + FP32 refine), 1000^3 R=32 nonneg CPD-ALS"
+# Sweeps the FP64 ALS needs to reach the target on this workload (measured with the FP32
+# plain form, whose per-sweep relative error follows the FP64 oracle within 1e-4).
+SWEEPS_TO_TARGET_FP64 = None   # filled from the plain-form run when available
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", os.environ.get("LOCAL_RANK", "0")],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sweep_seconds(X_host_flat, dims, R, init, threads, sweeps=1):
+    """One (or more) full-size FP64 ALS sweeps of the OpenMP restatement; seconds per sweep."""
+    from oracle import omp
+    t = time.perf_counter()
+    fs, st, tr = omp.cpd_als(X_host_flat, dims, R, init, max_iter=sweeps, threshold_error=0.0,
+                             nthreads=threads)
+    return (time.perf_counter() - t) / sweeps, st
+
+
+def run_reference(args):
+    """CPU restatement of the reference (oracle/cpd_omp.c, FP64, all host threads)."""
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    ge = __import__("__graft_entry__")
+    pkg = ge.load_package()
+    from partensor_toolbox_gb300 import datagen as dg
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    p = dg.make_cpd_problem(DIMS, RANK, seed=SEED, init_seed=INIT_SEED, snr_db=SNR_DB,
+                            equalize_columns=True, device=dev)
+    Xh = p.X.cpu().numpy()
+    init = [f.cpu().numpy() for f in p.init_factors]
+    del p
+    threads = os.cpu_count() or 1
+    sweeps = args.sweeps_to_target
+    times = []
+    for _ in range(max(0, args.warmup_ref)):
+        cpu_sweep_seconds(Xh, DIMS, RANK, init, threads)
+    for _ in range(args.steps):
+        s, _ = cpu_sweep_seconds(Xh, DIMS, RANK, init, threads)
+        times.append(s)
+    per_sweep = statistics.mean(times)
+    value = per_sweep * sweeps
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sweep * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "cpd_als 1000x1000x1000 R=32 30dB nonneg",
+                                            "rank": RANK, "dims": DIMS, "l2": "inputs > L2"},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
+                             "sample": f"1 full-size FP64 ALS sweep per step (OpenMP restatement of "
+                                       f"CpdOpenMP, oracle/cpd_omp.c), x {sweeps} sweeps to target"},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    ge = __import__("__graft_entry__")
+    pkg = ge.load_package()
+    from partensor_toolbox_gb300 import datagen as dg
+    dims, R = DIMS if not args.small else [200, 200, 200], RANK
+    p = dg.make_cpd_problem(dims, R, seed=SEED, init_seed=INIT_SEED, snr_db=SNR_DB, equalize_columns=True,
+                            device="cuda")
+    target = p.noise_rel + 1e-3
+    init = [f.cpu().numpy() for f in p.init_factors]
+    ctx = pkg.Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    Xb = pkg.Tensor(ctx, (p.X.data_ptr(), dims), precision="bf16")
+    Xf = pkg.Tensor(ctx, (p.X.data_ptr(), dims), precision="f32")
+    max_iter = args.max_iter
+
+    def solve(form):
+        if form == "bf16":
+            o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target, precision="bf16",
+                            refine_sweeps=1)
+            return pkg.cpd_resident(ctx, Xb, R, o, init, refine=Xf)
+        o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target)
+        return pkg.cpd_resident(ctx, Xf, R, o, init)
+
+    def timed(form, k, stats=False):
+        sts = []
+        torch.cuda.synchronize()
+        _barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if stats:
+            ctx.enable_stats(True)
+            ctx.reset_stats()
+        e0.record(stream)
+        for _ in range(k):
+            sts.append(solve(form))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        _barrier(ws)
+        st_k = ctx.stats() if stats else None
+        if stats:
+            ctx.enable_stats(False)
+        ms = e0.elapsed_time(e1) / k
+        return ms, sts, st_k
+
+    for _ in range(args.warmup):
+        solve("bf16")
+    solve("f32")
+    clk = ClockSampler()
+    clk.start()
+    ms_b, st_b, kst = timed("bf16", args.steps, stats=True)
+    clocks = clk.stop()
+    ms_f, st_f, _ = timed("f32", max(1, args.steps_plain))
+    ms_b = _max_over_ranks(ms_b, ws)
+    ms_f = _max_over_ranks(ms_f, ws)
+
+    # roofline of the dominant kernel (MTTKRP, tensor-core form)
+    peak, peak_kind = _peaks()
+    launches = max(1, kst["mttkrp_launches"])
+    per_launch_ms = kst["mttkrp_ms"] / launches
+    bytes_per_launch = kst["mttkrp_bytes"] / launches
+    achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
+
+    # end-to-end through the one-call C ABI with a pinned host FP64 buffer
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty(p.X.numel(), dtype=torch.float64, pin_memory=True)
+        host.copy_(p.X)
+        hnp = host.numpy()
+        o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target, precision="bf16", refine_sweeps=1)
+        pkg.cpd(hnp, R, o, init, dims=dims, ctx=ctx)   # warm-up
+        ts = []
+        for _ in range(max(1, args.steps_e2e)):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            st_e = pkg.cpd(hnp, R, o, init, dims=dims, ctx=ctx)
+            ts.append(time.perf_counter() - t)
+        e2e = {"value": _max_over_ranks(statistics.mean(ts), ws), "unit": "s",
+               "h2d_bytes_per_step": int(hnp.nbytes + sum(f.nbytes for f in init)),
+               "d2h_bytes_per_step": int(sum(f.nbytes for f in st_e.factors)),
+               "rel_err": st_e.rel_costFunction}
+        del host
+
+    sweeps_plain = st_f[-1].ao_iter
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        Xh = p.X.cpu().numpy()
+        threads = os.cpu_count() or 1
+        s_sweep, _ = cpu_sweep_seconds(Xh, dims, R, init, threads)
+        cpu = {"value": s_sweep * sweeps_plain, "unit": "s", "cores": threads, "kind": "port",
+               "sample": f"1 full-size FP64 ALS sweep of the OpenMP restatement of CpdOpenMP "
+                         f"(oracle/cpd_omp.c) = {s_sweep:.2f} s, x {sweeps_plain} sweeps to target "
+                         f"(the FP32 plain form's count)"}
+        del Xh
+
+    last_b, last_f = st_b[-1], st_f[-1]
+    line = {
+        "metric": METRIC, "value": ms_b / 1e3, "unit": "s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic (seeded U[0,1] factors, 30 dB Gaussian noise)",
+        "config": {"workload": f"cpd_als {dims[0]}x{dims[1]}x{dims[2]} R={R} 30dB nonneg, to target",
+                   "rank": R, "dims": dims, "target_rel": target, "noise_floor_rel": p.noise_rel,
+                   "l2": "inputs (2 GB BF16 / 4 GB FP32) > 129 MB L2, no flush",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "converged": bool(last_b.rel_costFunction <= target),
+        "final_rel_err": last_b.rel_costFunction,
+        "sweeps": last_b.ao_iter, "refine_sweeps": last_b.refine_sweeps_done,
+        "nesterov_iters_total": last_b.nesterov_iters_total,
+        "plain_fp32": {"value": ms_f / 1e3, "unit": "s", "sweeps": sweeps_plain,
+                       "final_rel_err": last_f.rel_costFunction,
+                       "converged": bool(last_f.rel_costFunction <= target)},
+        "speedup_vs_plain_fp32": (ms_f / ms_b) if ms_b > 0 else None,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "MTTKRP (tcgen05, BF16 storage) incl. split-K reduction",
+                     "launches": kst["mttkrp_launches"], "ms_per_launch": per_launch_ms,
+                     "bytes_per_launch": bytes_per_launch},
+        "gpu_launches": kst["launches"],
+        "clocks": clocks,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    Xb.close()
+    Xf.close()
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--steps-plain", type=int, default=2)
+    ap.add_argument("--steps-e2e", type=int, default=2)
+    ap.add_argument("--max-iter", type=int, default=200)
+    ap.add_argument("--small", action="store_true", help="200^3 smoke configuration")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--warmup-ref", type=int, default=0)
+    ap.add_argument("--sweeps-to-target", type=int, default=20)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

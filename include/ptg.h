@@ -63,7 +63,15 @@ int ptg_ctx_create(int device, ptg_ctx **out);
 int ptg_ctx_destroy(ptg_ctx *ctx);
 /* Run all work of this context on a caller-provided cudaStream_t (NULL: own stream). */
 int ptg_ctx_set_stream(ptg_ctx *ctx, void *cuda_stream);
+/* Waits for the context's stream; also reports a device-side error (PTG_ERR_TIMEOUT from a
+ * bounded wait inside a kernel) raised since the last check, and clears it. */
 int ptg_ctx_synchronize(ptg_ctx *ctx);
+
+/* Context options (GB300 knobs, no reference counterpart). */
+typedef enum {
+  PTG_OPT_MTTKRP_IMPL = 1 /* 0: auto (tensor cores for BF16 storage), 1: CUDA cores, 2: tensor cores */
+} ptg_option;
+int ptg_ctx_set_option(ptg_ctx *ctx, int option, long long value);
 
 /* Kernel statistics of a context (no counterpart in the reference, which only has a
  * host stopwatch, include/Timers.hpp:39-142).  When enabled, every MTTKRP launch is

@@ -13,11 +13,13 @@ MAX_ORDER = 8
 
 PTG_OK, PTG_ERR_INVALID, PTG_ERR_CUDA, PTG_ERR_OOM, PTG_ERR_UNSUPPORTED, PTG_ERR_TIMEOUT, PTG_ERR_NUMERIC = range(7)
 PTG_F32, PTG_BF16 = 0, 1
+PTG_OPT_MTTKRP_IMPL = 1
+MTTKRP_IMPLS = {"auto": 0, "cuda_cores": 1, "tensor_cores": 2}
 
 # every symbol include/ptg.h declares
 EXPORTS = [
     "ptg_last_error", "ptg_version", "ptg_ctx_create", "ptg_ctx_destroy", "ptg_ctx_set_stream",
-    "ptg_ctx_synchronize", "ptg_ctx_enable_stats", "ptg_ctx_get_stats", "ptg_ctx_reset_stats",
+    "ptg_ctx_synchronize", "ptg_ctx_set_option", "ptg_ctx_enable_stats", "ptg_ctx_get_stats", "ptg_ctx_reset_stats",
     "ptg_tensor_create", "ptg_tensor_destroy", "ptg_tensor_norms",
     "ptg_mttkrp", "ptg_cpd_default_options", "ptg_cpd_als", "ptg_cpd",
 ]
@@ -75,6 +77,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ptg_ctx_destroy.argtypes = [vp]
     lib.ptg_ctx_set_stream.argtypes = [vp, vp]
     lib.ptg_ctx_synchronize.argtypes = [vp]
+    lib.ptg_ctx_set_option.argtypes = [vp, ctypes.c_int, ctypes.c_longlong]
     lib.ptg_ctx_enable_stats.argtypes = [vp, ctypes.c_int]
     lib.ptg_ctx_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     lib.ptg_ctx_reset_stats.argtypes = [vp]

@@ -93,6 +93,10 @@ class Context:
     def synchronize(self):
         check(self._lib.ptg_ctx_synchronize(self.handle))
 
+    def set_mttkrp_impl(self, impl: str):
+        """"auto" (tensor cores for BF16 storage), "cuda_cores" or "tensor_cores"."""
+        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_MTTKRP_IMPL, _lib.MTTKRP_IMPLS[impl]))
+
     def enable_stats(self, on: bool = True):
         check(self._lib.ptg_ctx_enable_stats(self.handle, int(on)))
 

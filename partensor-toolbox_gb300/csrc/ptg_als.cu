@@ -122,7 +122,7 @@ struct Runner {
     int hi[2 * PTG_MAX_ORDER];
     PTG_CUDA(cudaMemcpyAsync(hd, b.dsc, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, S));
     PTG_CUDA(cudaMemcpyAsync(hi, b.isc, sizeof(int) * 2 * N, cudaMemcpyDeviceToHost, S));
-    PTG_CUDA(cudaStreamSynchronize(S));
+    PTG_TRY(check_device_error(ctx));
     const int last = N - 1;
     const double f2 = frob - 2.0 * hd[4 * last] + hd[4 * last + 1];
     if (!std::isfinite(f2)) return set_error(PTG_ERR_NUMERIC, "cost is NaN or Inf");
@@ -142,7 +142,7 @@ struct Runner {
     count_launches(ctx, 1);
     double h[2];
     PTG_CUDA(cudaMemcpyAsync(h, b.dsc + 2, sizeof(h), cudaMemcpyDeviceToHost, S));
-    PTG_CUDA(cudaStreamSynchronize(S));
+    PTG_TRY(check_device_error(ctx));
     const double f2 = frob + h[1] - 2.0 * h[0];
     if (!std::isfinite(f2)) return set_error(PTG_ERR_NUMERIC, "cost is NaN or Inf");
     *f_out = std::sqrt(std::max(f2, 0.0));

@@ -90,6 +90,18 @@ int stats_resolve(ptg_ctx *ctx) {
   return PTG_OK;
 }
 
+int check_device_error(ptg_ctx *ctx) {
+  int h = 0;
+  PTG_CUDA(cudaMemcpyAsync(&h, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  PTG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (h != 0) {
+    PTG_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
+    PTG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return set_error(h, "a device-side bounded wait gave up (kernel returned early)");
+  }
+  return PTG_OK;
+}
+
 namespace {
 
 // FP64 ColMajor source chunk -> padded storage, with FP64 partial sums of squares of the
@@ -194,6 +206,8 @@ int ptg_ctx_create(int device, ptg_ctx **out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc(&c->dev_err, 256);
+  if (e == cudaSuccess) e = cudaMemset(c->dev_err, 0, 256);
   if (e != cudaSuccess) {
     ptg_ctx_destroy(c);
     return cuda_error(e, "ptg_ctx_create", __FILE__, __LINE__);
@@ -210,6 +224,7 @@ int ptg_ctx_destroy(ptg_ctx *c) {
   c->scratch.release();
   stats_resolve(c);
   for (cudaEvent_t e : c->stats.pool) cudaEventDestroy(e);
+  if (c->dev_err) cudaFree(c->dev_err);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->side) cudaStreamDestroy(c->side);
@@ -228,7 +243,19 @@ int ptg_ctx_synchronize(ptg_ctx *c) {
   if (!c) return set_error(PTG_ERR_INVALID, "ctx is NULL");
   PTG_CUDA(cudaSetDevice(c->device));
   PTG_CUDA(cudaStreamSynchronize(c->stream));
-  return PTG_OK;
+  return check_device_error(c);
+}
+
+int ptg_ctx_set_option(ptg_ctx *c, int option, long long value) {
+  if (!c) return set_error(PTG_ERR_INVALID, "ctx is NULL");
+  switch (option) {
+    case PTG_OPT_MTTKRP_IMPL:
+      if (value < 0 || value > 2) return set_error(PTG_ERR_INVALID, "MTTKRP impl must be 0, 1 or 2");
+      c->mttkrp_impl = (int)value;
+      return PTG_OK;
+    default:
+      return set_error(PTG_ERR_INVALID, "unknown option");
+  }
 }
 
 int ptg_ctx_enable_stats(ptg_ctx *c, int enable) {

@@ -61,6 +61,8 @@ struct ptg_ctx {
   ptg::DevBuf scratch;                // split-K partials and other temporaries
   int nnls_cluster = 0;               // cluster size the NNLS kernel launched with (0 = unknown)
   ptg_ctx_stats stats;
+  int mttkrp_impl = 0;                // PTG_OPT_MTTKRP_IMPL
+  int *dev_err = nullptr;             // device error word written by bounded waits
 };
 
 struct ptg_tensor {
@@ -101,6 +103,12 @@ Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors,
 // row-major [q_write][R].
 int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                        cudaStream_t stream);
+
+// tcgen05 (tensor-core) form of contraction_launch; BF16 storage only.
+int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
+                          cudaStream_t stream);
+// Reads and clears the device error word (synchronises the stream first).
+int check_device_error(ptg_ctx *ctx);
 
 // Statistics helpers: count kernel launches; bracket a contraction with events.
 inline void count_launches(ptg_ctx *ctx, int n) { ctx->stats.launches += n; }

@@ -462,6 +462,8 @@ int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, 
   int rc;
   if (t->dtype == PTG_F32)
     rc = launch_typed<float>(ctx, t, c, R, out, stream);
+  else if (t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 256)
+    rc = tc_contraction_launch(ctx, t, c, R, out, stream);
   else if (t->dtype == PTG_BF16)
     rc = launch_typed<__nv_bfloat16>(ctx, t, c, R, out, stream);
   else

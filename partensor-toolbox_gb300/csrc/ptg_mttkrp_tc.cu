@@ -1,0 +1,522 @@
+// Dense MTTKRP on the 5th-generation tensor cores (tcgen05, kind::f16, BF16 x BF16 -> FP32).
+//
+// Same contraction as the CUDA-core kernel (ptg_mttkrp.cu): the BF16 tensor viewed as
+// [P, Q, S], out[q, r] = sum_{p,s} X[p,q,s] KRb[p,r] KRa[s,r].  One CTA per SM, warp
+// specialised:
+//   warp 0      TMA producer: 128 x 64 BF16 tiles of X into a ring of shared-memory stages
+//               (128-byte swizzle; K-major for modes n >= 1, MN-major for mode 0);
+//   warp 1      allocates TMEM and issues tcgen05.mma (M=128, N=R padded to 16, K=16) from
+//               one elected lane; each q-tile of the CTA accumulates in its own TMEM columns;
+//   warps 2..5  build the R x 64 Khatri-Rao tile of every K-block in shared memory (BF16,
+//               swizzled K-major), then drain TMEM (tcgen05.ld) into the split-K partials.
+// Every mbarrier wait is bounded: on timeout the kernel raises an error word and returns
+// after releasing its TMEM.
+#include <cuda.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <mutex>
+
+#include "ptg_internal.h"
+
+namespace ptg {
+namespace {
+
+constexpr int TC_BM = 128;         // q rows per tile (MMA M)
+constexpr int TC_BK = 64;          // contraction elements per K-block (one 128-byte row)
+constexpr int TC_STAGES = 8;       // X tile ring
+constexpr int TC_KSTAGES = 4;      // Khatri-Rao tile ring
+constexpr int TC_THREADS = 192;
+constexpr int TC_ATILE = TC_BM * TC_BK * 2;   // 16 KB
+constexpr uint32_t kSpinLimit = 1u << 26;
+
+struct KrDevTc {
+  int n;
+  uint32_t ext[PTG_MAX_ORDER];
+  uint32_t valid[PTG_MAX_ORDER];
+  const float *fac[PTG_MAX_ORDER];
+};
+
+struct TcParams {
+  int64_t P, Q, S;
+  int64_t kblocks_total, kblocks_per_split, pblocks;
+  int qtiles, mt_per_cta;
+  int N;          // MMA N: rank padded to a multiple of 16
+  int R;
+  int mmajor;
+  uint32_t tmem_cols;
+  KrDevTc before, after;
+  float *partial;  // [nsplit][Q][N]
+  int *err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait; false when it gave up (or another role already gave up).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 1023) == 1023 && *abort) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1,
+                                            int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor (tcgen05): start, leading/stride byte offsets, fixed
+// version bits 46-48 = 0b001, 128-byte swizzle (layout type 2 in bits 61-63).
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Khatri-Rao values of one side for linear index `lin`, 8 consecutive columns from c.
+__device__ __forceinline__ void kr8(const KrDevTc &s, uint32_t lin, int R, int c, float *v) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) v[j] = 1.0f;
+  for (int f = 0; f < s.n; ++f) {
+    const uint32_t e = s.ext[f];
+    const uint32_t d = lin % e;
+    lin /= e;
+    if (d >= s.valid[f]) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = 0.0f;
+      return;
+    }
+    const float *row = s.fac[f] + (size_t)d * R;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] *= (c + j < R) ? __ldg(row + c + j) : 0.0f;
+  }
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  // 1024-byte aligned carve: A ring, K ring, barriers
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int N = prm.N;
+  const int KTILE = N * 128;                       // R_pad rows of 128 bytes
+  uint8_t *aring = base;
+  uint8_t *kring = aring + TC_STAGES * TC_ATILE;
+  uint64_t *bars = (uint64_t *)(kring + TC_KSTAGES * KTILE);
+  uint64_t *full_a = bars, *empty_a = bars + TC_STAGES;
+  uint64_t *full_k = empty_a + TC_STAGES, *empty_k = full_k + TC_KSTAGES;
+  uint64_t *done = empty_k + TC_KSTAGES;
+  uint32_t *tmem_slot = (uint32_t *)(done + 1);
+  volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int qgroup = blockIdx.x, split = blockIdx.y;
+  const int qt0 = qgroup * prm.mt_per_cta;
+  const int nqt = min(prm.mt_per_cta, prm.qtiles - qt0);
+  const int64_t kb0 = (int64_t)split * prm.kblocks_per_split;
+  const int64_t kb1 = min(prm.kblocks_total, kb0 + prm.kblocks_per_split);
+  const int nkb = kb1 > kb0 ? (int)(kb1 - kb0) : 0;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < TC_STAGES; ++i) {
+      mbar_init(&full_a[i], 1);
+      mbar_init(&empty_a[i], 1);
+    }
+    for (int i = 0; i < TC_KSTAGES; ++i) {
+      mbar_init(&full_k[i], 128);
+      mbar_init(&empty_k[i], 1);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(prm.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  // idesc: D=F32 (bit 4), A=BF16 (bit 7), B=BF16 (bit 10), A major (bit 15), N>>3 (17-22), M>>4 (24-28)
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)prm.mmajor << 15) |
+                         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0 && nkb > 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int64_t t = kb0 + kb;
+        for (int m = 0; m < nqt; ++m) {
+          if (!mbar_wait(&empty_a[stage], phase ^ 1, abort_flag)) {
+            *abort_flag = 1;
+            atomicExch(prm.err, PTG_ERR_TIMEOUT);
+            goto producer_done;
+          }
+          mbar_expect_tx(&full_a[stage], TC_ATILE);
+          uint8_t *dst = aring + stage * TC_ATILE;
+          const int q = (qt0 + m) * TC_BM;
+          if (prm.mmajor) {
+            const int s0 = (int)(t * TC_BK);
+            tma_load_2d(dst, &tmap, &full_a[stage], q, s0);
+            tma_load_2d(dst + TC_ATILE / 2, &tmap, &full_a[stage], q + 64, s0);
+          } else {
+            const int s = (int)(t / prm.pblocks);
+            const int p0 = (int)((t % prm.pblocks) * TC_BK);
+            tma_load_3d(dst, &tmap, &full_a[stage], p0, q, s);
+          }
+          if (++stage == TC_STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+    producer_done:;
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int stage = 0, kst = 0;
+      uint32_t phase = 0, kphase = 0;
+      bool ok = true;
+      for (int kb = 0; kb < nkb && ok; ++kb) {
+        if (!mbar_wait(&full_k[kst], kphase, abort_flag)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t kaddr = smem_u32(kring + kst * KTILE);
+        for (int m = 0; m < nqt; ++m) {
+          if (!mbar_wait(&full_a[stage], phase, abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t aaddr = smem_u32(aring + stage * TC_ATILE);
+#pragma unroll
+          for (int kk = 0; kk < TC_BK / 16; ++kk) {
+            const uint64_t ad = prm.mmajor ? smem_desc_sw128(aaddr + kk * 2048, TC_ATILE / 2, 1024)
+                                           : smem_desc_sw128(aaddr + kk * 32, 16, 1024);
+            const uint64_t bd = smem_desc_sw128(kaddr + kk * 32, 16, 1024);
+            umma_bf16(tmem_base + (uint32_t)(m * N), ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+          }
+          umma_commit(&empty_a[stage]);
+          if (++stage == TC_STAGES) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        if (!ok) break;
+        umma_commit(&empty_k[kst]);
+        if (++kst == TC_KSTAGES) {
+          kst = 0;
+          kphase ^= 1;
+        }
+      }
+      if (!ok) {
+        *abort_flag = 1;
+        atomicExch(prm.err, PTG_ERR_TIMEOUT);
+      }
+      umma_commit(done);   // arrives once every MMA issued above has completed
+    }
+  } else {
+    // ---------------- Khatri-Rao builders (128 threads) ----------------
+    const int tb = threadIdx.x - 64;
+    const int k = tb & 63, nhalf = tb >> 6;
+    const int ncols = N / 2;
+    int kst = 0;
+    uint32_t kphase = 0;
+    for (int kb = 0; kb < nkb; ++kb) {
+      if (!mbar_wait(&empty_k[kst], kphase ^ 1, abort_flag)) {
+        *abort_flag = 1;
+        atomicExch(prm.err, PTG_ERR_TIMEOUT);
+        break;
+      }
+      const int64_t t = kb0 + kb;
+      uint8_t *kt = kring + kst * KTILE;
+      // linear indices of this thread's row of the K-block
+      bool valid;
+      uint32_t lin_b = 0, lin_a;
+      if (prm.mmajor) {
+        const int64_t s = t * TC_BK + k;
+        valid = s < prm.S;
+        lin_a = (uint32_t)s;
+      } else {
+        const int64_t s = t / prm.pblocks;
+        const int64_t p = (t % prm.pblocks) * TC_BK + k;
+        valid = p < prm.P;
+        lin_a = (uint32_t)s;
+        lin_b = (uint32_t)p;
+      }
+      for (int c = nhalf * ncols; c < (nhalf + 1) * ncols; c += 8) {
+        float va[8], vb[8];
+        if (valid) {
+          kr8(prm.after, lin_a, prm.R, c, va);
+          if (!prm.mmajor) {
+            kr8(prm.before, lin_b, prm.R, c, vb);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) va[j] *= vb[j];
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) va[j] = 0.0f;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int n = c + j;
+          const uint32_t off = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128 + ((((k >> 3) ^ (n & 7)) & 7) << 4) +
+                                          (k & 7) * 2);
+          *reinterpret_cast<__nv_bfloat16 *>(kt + off) = __float2bfloat16_rn(va[j]);
+        }
+      }
+      fence_async_smem();
+      mbar_arrive(&full_k[kst]);
+      if (++kst == TC_KSTAGES) {
+        kst = 0;
+        kphase ^= 1;
+      }
+    }
+    // ---------------- epilogue: TMEM -> partials ----------------
+    const bool have = (nkb > 0) && mbar_wait(done, 0, abort_flag) && !*abort_flag;
+    tc_fence_after();
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;
+    for (int m = 0; m < nqt; ++m) {
+      const int64_t q = (int64_t)(qt0 + m) * TC_BM + row;
+      float *dst = prm.partial + ((int64_t)split * prm.Q + q) * N;
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16];
+        if (have) {
+          tmem_ld16(tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(m * N + c0), v);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) v[i] = 0.0f;
+        }
+        if (q < prm.Q) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 4)
+            *reinterpret_cast<float4 *>(dst + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(prm.tmem_cols)
+                 : "memory");
+  }
+}
+
+__global__ void tc_reduce_kernel(const float *__restrict__ partial, int nsplit, int64_t Q, int N, int64_t q_write,
+                                 int R, float *__restrict__ out) {
+  const int64_t n = q_write * R;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = idx / R;
+    const int c = (int)(idx % R);
+    float s = 0.0f;
+    for (int sp = 0; sp < nsplit; ++sp) s += partial[((int64_t)sp * Q + q) * N + c];
+    out[idx] = s;
+  }
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+size_t tc_smem_bytes(int N) {
+  return 1024 /*alignment slack*/ + (size_t)TC_STAGES * TC_ATILE + (size_t)TC_KSTAGES * N * 128 +
+         sizeof(uint64_t) * (2 * TC_STAGES + 2 * TC_KSTAGES + 1) + 16;
+}
+
+}  // namespace
+
+int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
+                          cudaStream_t stream) {
+  if (t->dtype != PTG_BF16) return set_error(PTG_ERR_INVALID, "internal: tcgen05 path needs BF16 storage");
+  if (R > 256) return set_error(PTG_ERR_UNSUPPORTED, "tcgen05 MTTKRP: rank > 256");
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return set_error(PTG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  const bool mmajor = (c.P == 1);
+  if (mmajor && (c.Q % 8) != 0) return set_error(PTG_ERR_INVALID, "internal: Q must be a multiple of 8");
+  if (c.Q > 0x7fffffffLL || c.S > 0x7fffffffLL || c.P > 0x7fffffffLL)
+    return set_error(PTG_ERR_UNSUPPORTED, "tcgen05 MTTKRP: extent exceeds 2^31");
+  TcParams prm{};
+  prm.P = c.P;
+  prm.Q = c.Q;
+  prm.S = c.S;
+  prm.N = (R + 15) / 16 * 16;
+  prm.R = R;
+  prm.mmajor = mmajor ? 1 : 0;
+  auto cp = [](const KrSide &s) {
+    KrDevTc d{};
+    d.n = s.n;
+    for (int i = 0; i < s.n; ++i) {
+      d.ext[i] = (uint32_t)s.ext[i];
+      d.valid[i] = (uint32_t)s.valid[i];
+      d.fac[i] = s.fac[i];
+    }
+    return d;
+  };
+  prm.before = cp(c.before);
+  prm.after = cp(c.after);
+  prm.qtiles = (int)((c.Q + TC_BM - 1) / TC_BM);
+  int mt = std::max(1, 512 / prm.N);
+  mt = std::min(mt, prm.qtiles);
+  const int qgroups_min = (prm.qtiles + mt - 1) / mt;
+  // balance q-tiles over the groups
+  mt = (prm.qtiles + qgroups_min - 1) / qgroups_min;
+  prm.mt_per_cta = mt;
+  const int qgroups = (prm.qtiles + mt - 1) / mt;
+  uint32_t cols = 32;
+  while (cols < (uint32_t)(mt * prm.N)) cols <<= 1;
+  prm.tmem_cols = cols;
+  if (mmajor) {
+    prm.pblocks = 1;
+    prm.kblocks_total = (c.S + TC_BK - 1) / TC_BK;
+  } else {
+    prm.pblocks = (c.P + TC_BK - 1) / TC_BK;
+    prm.kblocks_total = c.S * prm.pblocks;
+  }
+  int64_t nsplit = std::max<int64_t>(1, ctx->sm_count / qgroups);
+  nsplit = std::min<int64_t>(nsplit, prm.kblocks_total);
+  prm.kblocks_per_split = (prm.kblocks_total + nsplit - 1) / nsplit;
+  nsplit = (prm.kblocks_total + prm.kblocks_per_split - 1) / prm.kblocks_per_split;
+
+  // tensor map over the BF16 tensor
+  CUtensorMap map;
+  CUresult r;
+  if (mmajor) {
+    cuuint64_t gdim[2] = {(cuuint64_t)c.Q, (cuuint64_t)c.S};
+    cuuint64_t gstride[1] = {(cuuint64_t)c.Q * 2};
+    cuuint32_t box[2] = {64, 64};
+    cuuint32_t es[2] = {1, 1};
+    r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, t->data, gdim, gstride, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  } else {
+    cuuint64_t gdim[3] = {(cuuint64_t)c.P, (cuuint64_t)c.Q, (cuuint64_t)c.S};
+    cuuint64_t gstride[2] = {(cuuint64_t)c.P * 2, (cuuint64_t)c.P * c.Q * 2};
+    cuuint32_t box[3] = {64, 128, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, t->data, gdim, gstride, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  }
+  if (r != CUDA_SUCCESS) {
+    char buf[128];
+    snprintf(buf, sizeof(buf), "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return set_error(PTG_ERR_CUDA, buf);
+  }
+  // scratch: split-K partials
+  const size_t part_bytes = (size_t)nsplit * c.Q * prm.N * sizeof(float);
+  PTG_TRY(ctx->scratch.ensure(part_bytes));
+  prm.partial = reinterpret_cast<float *>(ctx->scratch.ptr);
+  prm.err = ctx->dev_err;
+  const size_t smem = tc_smem_bytes(prm.N);
+  PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((unsigned)qgroups, (unsigned)nsplit);
+  mttkrp_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(map, prm);
+  PTG_CUDA(cudaGetLastError());
+  const int64_t n = c.q_write * R;
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->sm_count * 8);
+  tc_reduce_kernel<<<std::max(blocks, 1), 256, 0, stream>>>(prm.partial, (int)nsplit, c.Q, prm.N, c.q_write, R,
+                                                            out);
+  PTG_CUDA(cudaGetLastError());
+  count_launches(ctx, 2);
+  return PTG_OK;
+}
+
+}  // namespace ptg

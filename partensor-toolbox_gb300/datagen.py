@@ -50,7 +50,9 @@ def make_cpd_problem(dims: Sequence[int], rank: int, seed: int, snr_db: float,
     ``snr_db`` dB SNR, sigma^2 = ||[[A]]||^2 / (prod(I) * 10^(snr/10)); initial factors
     i.i.d. U[0,1] (seed ``init_seed``, default seed+1).
 
-    ``equalize_columns`` rescales every column of every factor to unit norm.
+    ``equalize_columns`` rescales every column of a factor to the same norm (the mean
+    column norm of the draw, so the entries keep the U[0,1] scale that the reference's
+    absolute Nesterov tolerance, include/PARTENSOR_basic.hpp:188, is tuned for).
     ``collinearity=c`` makes the columns of each factor share a common component so the
     expected cosine between two columns is about c."""
     dims = [int(d) for d in dims]
@@ -68,7 +70,9 @@ def make_cpd_problem(dims: Sequence[int], rank: int, seed: int, snr_db: float,
                                                       (common - common.mean()).norm())
             A = A - A.min(0, keepdim=True).values      # back to nonnegative
         if equalize_columns:
-            A = A / A.norm(dim=0, keepdim=True)
+            # every column rescaled to the mean column norm of the draw (keeps the U[0,1] scale)
+            nrm = A.norm(dim=0, keepdim=True)
+            A = A * (nrm.mean() / nrm)
         facs.append(A)
     T = full_tensor(facs)
     t2 = float((T * T).sum())
