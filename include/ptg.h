@@ -171,6 +171,19 @@ int ptg_cpd(ptg_ctx *ctx, int order, const int64_t *dims, const double *host_ten
             const double *const *init_factors, double *const *out_factors,
             ptg_cpd_result *result, ptg_sweep_trace *trace);
 
+/* Dimension-tree CPD-ALS: partensor::cpdDimTree (include/CpdDimTree.hpp:809-1362, loop
+ * :317-401).  The modes are split at h = (1 + N)/2 (include/DimTrees.hpp:274-276); the two
+ * node tensors T_left [prod_{k<h} I_k x R] and T_right [prod_{k>=h} I_k x R] stay resident in
+ * HBM, so a sweep reads the tensor twice instead of N times.  Same arguments as
+ * ptg_cpd_als / ptg_cpd. */
+int ptg_cpd_dimtree_als(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int rank,
+                        const ptg_cpd_options *opts, const double *const *init_factors,
+                        double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace);
+int ptg_cpd_dimtree(ptg_ctx *ctx, int order, const int64_t *dims, const double *host_tensor,
+                    ptg_dtype dtype, int rank, const ptg_cpd_options *opts,
+                    const double *const *init_factors, double *const *out_factors,
+                    ptg_cpd_result *result, ptg_sweep_trace *trace);
+
 #ifdef __cplusplus
 }
 #endif

@@ -395,3 +395,96 @@ def congruence(A: Sequence[np.ndarray], B: Sequence[np.ndarray]) -> float:
         C *= np.abs(an.T @ bn)
     r, c = linear_sum_assignment(-C)
     return float(C[r, c].mean())
+
+
+# --------------------------------------------------------------------------------------
+# Dimension-tree CPD, include/CpdDimTree.hpp:317-401 with include/DimTrees.hpp
+# --------------------------------------------------------------------------------------
+
+def dimtree_split(order: int) -> int:
+    """Labels of the root's left child: the first (1 + L)/2 modes (DIM_HALF_SIZE,
+    include/DimTrees.hpp:274-276); 4-way gives {0,1} | {2,3}."""
+    return (1 + order) // 2
+
+
+def dimtree_partial(factors: Sequence[np.ndarray], X: np.ndarray, keep: Sequence[int]) -> np.ndarray:
+    """Partial MTTKRP of a tree node: X contracted with the factors of every mode not in
+    ``keep`` (TreeMode_N_Product + TTVs, include/DimTrees.hpp:669-800), returned as an
+    array of shape [I_keep..., R]."""
+    N = X.ndim
+    letters = "abcdefgh"[:N]
+    spec = letters + "," + ",".join(f"{letters[k]}z" for k in range(N) if k not in keep)
+    spec += "->" + "".join(letters[k] for k in keep) + "z"
+    return np.einsum(spec, X, *[factors[k] for k in range(N) if k not in keep], optimize=True)
+
+
+def dimtree_leaf_mttkrp(T: np.ndarray, factors: Sequence[np.ndarray], keep: Sequence[int], mode: int):
+    """Leaf step: the node tensor T [I_keep..., R] contracted with the node's other
+    factors (TTVs with TensorPartialProduct_R, include/TensorOperations.hpp:196-213)."""
+    letters = "abcdefgh"[:len(keep)]
+    pos = list(keep).index(mode)
+    spec = letters + "z," + ",".join(f"{letters[i]}z" for i, k in enumerate(keep) if k != mode)
+    spec += "->" + letters[pos] + "z"
+    return np.einsum(spec, T, *[factors[k] for k in keep if k != mode], optimize=True)
+
+
+def cpd_dimtree_als(X: np.ndarray, R: int, options: Optional[Options] = None,
+                    factors_init: Optional[Sequence[np.ndarray]] = None) -> Status:
+    """CPD_DIMTREE::als (include/CpdDimTree.hpp:317-401): the same ALS sweep as cpd_als with
+    each MTTKRP taken from the node tensor of its half of the tree (the left node is
+    recomputed before mode 0 from the current right-half factors, the right node before the
+    first right-half mode from the updated left-half factors), the Gram-form cost
+    (include/CpdDimTree.hpp:156-160) and the dimension-tree Normalize
+    (include/Normalize.hpp:200-303, same arithmetic as Normalize)."""
+    X = np.asarray(X, dtype=np.float64)
+    N = X.ndim
+    last = N - 1
+    h = dimtree_split(N)
+    left, right = list(range(h)), list(range(h, N))
+    if options is None:
+        options = Options(order=N)
+    opts = dataclasses.replace(options, constraints=list(options.constraints))
+    st = Status(options=opts, factors=[np.array(f, dtype=np.float64, copy=True) for f in factors_init])
+    grams = [f.T @ f for f in st.factors]
+    all_orth, weight = True, 0
+    if opts.normalization:
+        all_orth, weight = choose_normalization_factor(opts.constraints)
+    st.frob_tns = square_norm(X)
+    st.f_value = cost_from_factors(X, st.factors)                      # CpdGen, :333-338
+    st.rel_costFunction = st.f_value / math.sqrt(st.frob_tns)
+    old_factors = None
+    while True:
+        st.ao_iter += 1
+        sweep = dict(iter=st.ao_iter, nesterov_iters=[], accel=None)
+        T = None
+        for i in range(N):
+            if i == 0:
+                T = dimtree_partial(st.factors, X, left)
+            elif i == h:
+                T = dimtree_partial(st.factors, X, right)
+            keep = left if i < h else right
+            M = dimtree_leaf_mttkrp(T, st.factors, keep, i)
+            Z = partial_cwise_prod(grams, i)
+            A_new, info = update_factor(i, opts.constraints[i], M, Z, st.factors[i],
+                                        opts.nesterov_delta_1, opts.nesterov_delta_2)
+            st.factors[i] = A_new
+            grams[i] = A_new.T @ A_new
+            sweep["nesterov_iters"].append(info.get("iters", 0))
+            if i == last:
+                f2 = st.frob_tns - 2.0 * (M * A_new).sum() + (Z * grams[last]).sum()
+                st.f_value = math.sqrt(max(f2, 0.0))
+        st.rel_costFunction = st.f_value / math.sqrt(st.frob_tns)
+        if opts.normalization and not all_orth:
+            normalize(weight, R, grams, st.factors)
+        sweep["f_value"] = st.f_value
+        sweep["rel"] = st.rel_costFunction
+        if st.ao_iter >= opts.max_iter or st.rel_costFunction < opts.threshold_error:
+            st.trace.append(sweep)
+            break
+        if opts.acceleration:
+            norm_factors = [f.copy() for f in st.factors]
+            if st.ao_iter > 1:
+                sweep["accel"] = _line_search_accel(X, st, old_factors, grams)
+            old_factors = norm_factors
+        st.trace.append(sweep)
+    return st

@@ -9,4 +9,4 @@ raises.
 """
 from . import _lib  # noqa: F401
 from .cpd import (CONSTANT, NONNEGATIVITY, ORTHOGONALITY, SPARSITY, UNCONSTRAINED, Context,  # noqa: F401
-                  Options, Status, Tensor, cpd, cpd_resident, default_context, mttkrp)
+                  Options, Status, Tensor, cpd, cpd_resident, cpdDimTree, default_context, mttkrp)

@@ -22,6 +22,7 @@ EXPORTS = [
     "ptg_ctx_synchronize", "ptg_ctx_set_option", "ptg_ctx_enable_stats", "ptg_ctx_get_stats", "ptg_ctx_reset_stats",
     "ptg_tensor_create", "ptg_tensor_destroy", "ptg_tensor_norms",
     "ptg_mttkrp", "ptg_cpd_default_options", "ptg_cpd_als", "ptg_cpd",
+    "ptg_cpd_dimtree_als", "ptg_cpd_dimtree",
 ]
 
 
@@ -92,6 +93,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ptg_cpd.argtypes = [vp, ctypes.c_int, i64p, dp, ctypes.c_int, ctypes.c_int,
                             ctypes.POINTER(CpdOptions), dpp, dpp, ctypes.POINTER(CpdResult),
                             ctypes.POINTER(SweepTrace)]
+    lib.ptg_cpd_dimtree_als.argtypes = lib.ptg_cpd_als.argtypes
+    lib.ptg_cpd_dimtree.argtypes = lib.ptg_cpd.argtypes
     for name in EXPORTS:
         if name not in ("ptg_last_error", "ptg_version", "ptg_cpd_default_options"):
             getattr(lib, name).restype = ctypes.c_int

@@ -206,8 +206,9 @@ def _status_from(opts: Options, outs, res: CpdResult, trace, ntrace) -> Status:
 
 
 def cpd_resident(ctx: Context, X: Tensor, R: int, options: Options, factorsInit: Sequence[np.ndarray],
-                 refine: Optional[Tensor] = None) -> Status:
-    """CPD-ALS on an HBM-resident tensor (``ptg_cpd_als``)."""
+                 refine: Optional[Tensor] = None, dimtree: bool = False) -> Status:
+    """CPD-ALS on an HBM-resident tensor (``ptg_cpd_als``; ``ptg_cpd_dimtree_als`` when
+    ``dimtree``)."""
     N = len(X.dims)
     inits = [np.asfortranarray(np.asarray(f, dtype=np.float64)) for f in factorsInit]
     outs = [np.zeros((X.dims[k], R), order="F") for k in range(N)]
@@ -216,13 +217,14 @@ def cpd_resident(ctx: Context, X: Tensor, R: int, options: Options, factorsInit:
     res = CpdResult()
     ntr = options.max_iter + max(0, options.refine_sweeps)
     trace = (SweepTrace * ntr)()
-    check(ctx._lib.ptg_cpd_als(ctx.handle, X.handle, refine.handle if refine else None, int(R),
-                               ctypes.byref(options.to_c()), ip, op, ctypes.byref(res), trace))
+    fn = ctx._lib.ptg_cpd_dimtree_als if dimtree else ctx._lib.ptg_cpd_als
+    check(fn(ctx.handle, X.handle, refine.handle if refine else None, int(R),
+             ctypes.byref(options.to_c()), ip, op, ctypes.byref(res), trace))
     return _status_from(options, outs, res, trace, res.ao_iter + res.refine_sweeps_done)
 
 
 def cpd(tnsX, R: int, options: Optional[Options] = None, factorsInit: Optional[Sequence[np.ndarray]] = None,
-        dims: Sequence[int] | None = None, ctx: Optional[Context] = None) -> Status:
+        dims: Sequence[int] | None = None, ctx: Optional[Context] = None, _dimtree: bool = False) -> Status:
     """partensor::cpd(execution::cuda, tnsX, R[, options][, factorsInit]) with a host
     FP64 tensor (``ptg_cpd``: upload, convert, solve, download in one call).
 
@@ -249,6 +251,15 @@ def cpd(tnsX, R: int, options: Optional[Options] = None, factorsInit: Optional[S
     res = CpdResult()
     ntr = options.max_iter + max(0, options.refine_sweeps)
     trace = (SweepTrace * ntr)()
-    check(ctx._lib.ptg_cpd(ctx.handle, N, d, _dptr(flat), DTYPES[options.precision], int(R),
-                           ctypes.byref(options.to_c()), ip, op, ctypes.byref(res), trace))
+    fn = ctx._lib.ptg_cpd_dimtree if _dimtree else ctx._lib.ptg_cpd
+    check(fn(ctx.handle, N, d, _dptr(flat), DTYPES[options.precision], int(R),
+             ctypes.byref(options.to_c()), ip, op, ctypes.byref(res), trace))
     return _status_from(options, outs, res, trace, res.ao_iter + res.refine_sweeps_done)
+
+
+def cpdDimTree(tnsX, R: int, options: Optional[Options] = None,
+               factorsInit: Optional[Sequence[np.ndarray]] = None, dims: Sequence[int] | None = None,
+               ctx: Optional[Context] = None) -> Status:
+    """partensor::cpdDimTree(execution::cuda, tnsX, R[, options][, factorsInit])
+    (include/CpdDimTree.hpp:809-1362) with a host FP64 tensor (``ptg_cpd_dimtree``)."""
+    return cpd(tnsX, R, options, factorsInit, dims=dims, ctx=ctx, _dimtree=True)

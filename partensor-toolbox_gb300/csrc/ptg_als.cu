@@ -29,13 +29,14 @@ struct AlsBuffers {
   float *gram[PTG_MAX_ORDER] = {nullptr};
   float *gacc[PTG_MAX_ORDER] = {nullptr};
   float *M = nullptr;
+  float *TL = nullptr, *TR = nullptr;   // dimension-tree node tensors (when used)
   float *gpart = nullptr;
   NnlsParams *np = nullptr;
   double *dsc = nullptr;  // [N][2]: <M, A>, sum(Z .* G); [N][2..3]: cost terms of a point
   int *isc = nullptr;     // [N][2]: iterations, repaired
   void *base = nullptr;
 
-  int alloc(const int64_t *dims, int order, int rank) {
+  int alloc(const int64_t *dims, int order, int rank, int64_t rows_left = 0, int64_t rows_right = 0) {
     N = order;
     R = rank;
     size_t off = 0;
@@ -60,6 +61,8 @@ struct AlsBuffers {
       gp = std::max(gp, gram_scratch_floats((int)dims[k], R));
     }
     const size_t o_M = take(sizeof(float) * maxrows * R);
+    const size_t o_TL = take(sizeof(float) * std::max<int64_t>(rows_left, 1) * R);
+    const size_t o_TR = take(sizeof(float) * std::max<int64_t>(rows_right, 1) * R);
     const size_t o_gp = take(sizeof(float) * gp);
     const size_t o_np = take(sizeof(NnlsParams));
     const size_t o_d = take(sizeof(double) * 4 * N);
@@ -78,6 +81,8 @@ struct AlsBuffers {
       gacc[k] = (float *)(b + o_ga[k]);
     }
     M = (float *)(b + o_M);
+    TL = (float *)(b + o_TL);
+    TR = (float *)(b + o_TR);
     gpart = (float *)(b + o_gp);
     np = (NnlsParams *)(b + o_np);
     dsc = (double *)(b + o_d);
@@ -95,6 +100,7 @@ struct Runner {
   AlsBuffers b;
   int weight = 0;
   bool all_orth = true;
+  bool dimtree = false;
   std::chrono::steady_clock::time_point t0;
 
   // one ALS sweep over all modes on tensor X; fills f (before acceleration) and per-mode
@@ -110,8 +116,17 @@ struct Runner {
       PTG_TRY(launch_eigen_bounds(b.gram, N, n, R, b.np, T));
       count_launches(ctx, 1);
       PTG_CUDA(cudaEventRecord(ctx->ev_join, T));
-      Contraction c = mttkrp_contraction(X, b.fac, n);
-      PTG_TRY(contraction_launch(ctx, X, c, R, b.M, S));
+      if (!dimtree) {
+        Contraction c = mttkrp_contraction(X, b.fac, n);
+        PTG_TRY(contraction_launch(ctx, X, c, R, b.M, S));
+      } else {
+        // node tensors: the left node before mode 0 (current right-half factors), the
+        // right node before the first right-half mode (updated left-half factors)
+        const int h = dimtree_split(N);
+        if (n == 0) PTG_TRY(contraction_launch(ctx, X, node_contraction(X, b.fac, true), R, b.TL, S));
+        if (n == h) PTG_TRY(contraction_launch(ctx, X, node_contraction(X, b.fac, false), R, b.TR, S));
+        PTG_TRY(launch_leaf_mttkrp(ctx, X, n < h ? b.TL : b.TR, b.fac, n, R, b.M, S));
+      }
       PTG_CUDA(cudaStreamWaitEvent(S, ctx->ev_join, 0));
       PTG_TRY(launch_nnls_full(ctx, b.M, b.fac[n], b.rows[n], R, b.np, (float)opt->nesterov_delta_1,
                                (float)opt->nesterov_delta_2, b.gram[n], b.dsc + 4 * n,
@@ -178,9 +193,12 @@ void ptg_cpd_default_options(int order, ptg_cpd_options *o) {
   o->cost_every_sweep = 1;
 }
 
-int ptg_cpd_als(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int rank,
-                const ptg_cpd_options *opts_in, const double *const *init_factors,
-                double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace) {
+}  // extern "C"
+
+static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int rank,
+                        const ptg_cpd_options *opts_in, const double *const *init_factors,
+                        double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace,
+                        bool dimtree) {
   if (!ctx || !X || !opts_in || !init_factors || !out_factors)
     return set_error(PTG_ERR_INVALID, "NULL argument");
   if (rank < 1 || rank > 64) return set_error(PTG_ERR_UNSUPPORTED, "rank must be in [1, 64]");
@@ -198,7 +216,8 @@ int ptg_cpd_als(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int
   ptg_cpd_options opt = *opts_in;
   Runner run{ctx, &opt};
   run.t0 = std::chrono::steady_clock::now();
-  PTG_TRY(run.b.alloc(X->dims, N, rank));
+  run.dimtree = dimtree;
+  PTG_TRY(run.b.alloc(X->dims, N, rank, dimtree ? node_rows(X, true) : 0, dimtree ? node_rows(X, false) : 0));
   AlsBuffers &b = run.b;
   cudaStream_t S = ctx->stream;
 
@@ -332,9 +351,26 @@ int ptg_cpd_als(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int
   return PTG_OK;
 }
 
-int ptg_cpd(ptg_ctx *ctx, int order, const int64_t *dims, const double *host_tensor, ptg_dtype dtype,
-            int rank, const ptg_cpd_options *opts, const double *const *init_factors,
-            double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace) {
+extern "C" {
+
+int ptg_cpd_als(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int rank,
+                const ptg_cpd_options *opts, const double *const *init_factors,
+                double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace) {
+  return cpd_als_impl(ctx, X, refine, rank, opts, init_factors, out_factors, result, trace, false);
+}
+
+int ptg_cpd_dimtree_als(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int rank,
+                        const ptg_cpd_options *opts, const double *const *init_factors,
+                        double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace) {
+  return cpd_als_impl(ctx, X, refine, rank, opts, init_factors, out_factors, result, trace, true);
+}
+
+}  // extern "C"
+
+static int cpd_host_impl(ptg_ctx *ctx, int order, const int64_t *dims, const double *host_tensor,
+                         ptg_dtype dtype, int rank, const ptg_cpd_options *opts,
+                         const double *const *init_factors, double *const *out_factors,
+                         ptg_cpd_result *result, ptg_sweep_trace *trace, bool dimtree) {
   if (!ctx || !dims || !host_tensor || !opts) return set_error(PTG_ERR_INVALID, "NULL argument");
   ptg_tensor *X = nullptr, *Xr = nullptr;
   const bool want_refine = dtype != PTG_F32 && opts->refine_sweeps > 0;
@@ -359,10 +395,26 @@ int ptg_cpd(ptg_ctx *ctx, int order, const int64_t *dims, const double *host_ten
     cudaStreamSynchronize(ctx->stream);
     cudaFree(dsrc);
   }
-  if (rc == PTG_OK) rc = ptg_cpd_als(ctx, X, Xr, rank, opts, init_factors, out_factors, result, trace);
+  if (rc == PTG_OK) rc = cpd_als_impl(ctx, X, Xr, rank, opts, init_factors, out_factors, result, trace, dimtree);
   ptg_tensor_destroy(X);
   ptg_tensor_destroy(Xr);
   return rc;
+}
+
+extern "C" {
+
+int ptg_cpd(ptg_ctx *ctx, int order, const int64_t *dims, const double *host_tensor, ptg_dtype dtype,
+            int rank, const ptg_cpd_options *opts, const double *const *init_factors,
+            double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace) {
+  return cpd_host_impl(ctx, order, dims, host_tensor, dtype, rank, opts, init_factors, out_factors, result,
+                       trace, false);
+}
+
+int ptg_cpd_dimtree(ptg_ctx *ctx, int order, const int64_t *dims, const double *host_tensor, ptg_dtype dtype,
+                    int rank, const ptg_cpd_options *opts, const double *const *init_factors,
+                    double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace) {
+  return cpd_host_impl(ctx, order, dims, host_tensor, dtype, rank, opts, init_factors, out_factors, result,
+                       trace, true);
 }
 
 }  // extern "C"

@@ -104,6 +104,13 @@ Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors,
 int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                        cudaStream_t stream);
 
+// Dimension tree (ptg_dimtree.cu): split point, node contraction, node size, leaf MTTKRP.
+int dimtree_split(int order);
+Contraction node_contraction(const ptg_tensor *t, const float *const *factors, bool left_node);
+int64_t node_rows(const ptg_tensor *t, bool left_node);
+int launch_leaf_mttkrp(ptg_ctx *ctx, const ptg_tensor *t, const float *T, const float *const *factors, int mode,
+                       int R, float *out, cudaStream_t stream);
+
 // tcgen05 (tensor-core) form of contraction_launch; BF16 storage only.
 int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                           cudaStream_t stream);

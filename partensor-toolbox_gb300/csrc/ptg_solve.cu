@@ -39,14 +39,44 @@ struct GramPtrs {
   const float *g[PTG_MAX_ORDER];
 };
 
-__device__ int sturm_count(const double *d, const double *e2, int n, double x) {
+// Sturm count (eigenvalues < x) of the symmetric tridiagonal (d, e^2) in FP32, ratio form
+// q_i = (d_i - x) - e_{i-1}^2 / q_{i-1}.
+__device__ int sturm_count_f32(const float *d, const float *e2, int n, float x) {
   int cnt = 0;
-  double q = d[0] - x;
-  if (q < 0.0) ++cnt;
+  float q = d[0] - x;
+  cnt += q < 0.0f;
   for (int i = 1; i < n; ++i) {
-    if (q == 0.0) q = 1e-300;
+    if (q == 0.0f) q = 1e-30f;
     q = (d[i] - x) - e2[i - 1] / q;
-    if (q < 0.0) ++cnt;
+    cnt += q < 0.0f;
+  }
+  return cnt;
+}
+
+// Same count in FP64 without divisions: the sign changes of the characteristic-polynomial
+// sequence p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}, rescaled by exact powers of two so
+// it neither overflows nor underflows (GB300's FP64 rate is low; a division costs ~10 FMAs).
+__device__ int sturm_count_f64(const double *d, const double *e2, int n, double x) {
+  double pm2 = 1.0, pm1 = d[0] - x;
+  int sprev = 1;                                  // sign of p_{-1} = 1
+  int s1 = pm1 < 0.0 ? -1 : (pm1 > 0.0 ? 1 : sprev);
+  int cnt = (s1 != sprev);
+  sprev = s1;
+  for (int i = 1; i < n; ++i) {
+    double p = (d[i] - x) * pm1 - e2[i - 1] * pm2;
+    const int s = p < 0.0 ? -1 : (p > 0.0 ? 1 : sprev);
+    cnt += (s != sprev);
+    sprev = s;
+    pm2 = pm1;
+    pm1 = p;
+    const double a = fabs(pm1);
+    if (a > 0x1p+256) {
+      pm1 *= 0x1p-256;
+      pm2 *= 0x1p-256;
+    } else if (a < 0x1p-256 && fabs(pm2) < 0x1p-256) {
+      pm1 *= 0x1p+256;
+      pm2 *= 0x1p+256;
+    }
   }
   return cnt;
 }
@@ -59,7 +89,7 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
   __shared__ double red[kEigThreads / 32];
   __shared__ double s_scalar[4];
   __shared__ double lohi[2][2];
-  __shared__ int firsthit[2];
+  __shared__ float df[kMaxR], e2f[kMaxR];
   const int tid = threadIdx.x;
   const int n = R;
 
@@ -140,30 +170,53 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
     hi += pad;
     lohi[0][0] = lo; lohi[0][1] = hi;   // smallest eigenvalue
     lohi[1][0] = lo; lohi[1][1] = hi;   // largest eigenvalue
+    s_scalar[1] = fmax(fabs(lo), fabs(hi));   // ||T|| bound
+  }
+  for (int i = tid; i < n; i += blockDim.x) {
+    df[i] = (float)d[i];
+    e2f[i] = (float)e2[i];
   }
   __syncthreads();
 
-  // ---- multisection: threads 0..127 bracket the smallest, 128..255 the largest ----
-  const int which = tid >> 7;      // 0: min, 1: max
-  const int j = tid & 127;
-  const int target = which == 0 ? 1 : n;  // count(x) >= target  <=>  x > lambda
-  for (int round = 0; round < 12; ++round) {
-    const double lo = lohi[which][0], hi = lohi[which][1];
-    const double x = lo + (hi - lo) * (double)(j + 1) / 129.0;
-    const int hit = sturm_count(d, e2, n, x) >= target;
-    if (j == 0) firsthit[which] = 128;
-    __syncthreads();
-    if (hit) atomicMin(&firsthit[which], j);
-    __syncthreads();
-    if (j == 0) {
-      const int f = firsthit[which];
-      const double nlo = (f == 0) ? lo : lo + (hi - lo) * (double)f / 129.0;
-      const double nhi = (f == 128) ? hi : lo + (hi - lo) * (double)(f + 1) / 129.0;
-      lohi[which][0] = nlo;
-      lohi[which][1] = nhi;
+  // ---- bisection: warp 0 brackets the smallest eigenvalue, warp 1 the largest, with a
+  // 32-way multisection per round: FP32 counts first, then FP64 counts on the widened
+  // FP32 bracket ----
+  if (tid < 64) {
+    const int which = tid >> 5;      // 0: min, 1: max
+    const int j = tid & 31;
+    const int target = which == 0 ? 1 : n;  // count(x) >= target  <=>  x > lambda
+    double lo = lohi[which][0], hi = lohi[which][1];
+    for (int round = 0; round < 6; ++round) {
+      const double x = lo + (hi - lo) * (double)(j + 1) / 33.0;
+      const bool hit = sturm_count_f32(df, e2f, n, (float)x) >= target;
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      const int f = m ? (__ffs(m) - 1) : 32;
+      const double nlo = (f == 0) ? lo : lo + (hi - lo) * (double)f / 33.0;
+      const double nhi = (f == 32) ? hi : lo + (hi - lo) * (double)(f + 1) / 33.0;
+      lo = nlo;
+      hi = nhi;
     }
-    __syncthreads();
+    // the FP32 counts are exact for a matrix within a few FP32 ulps of T (entrywise), so
+    // the eigenvalue lies within 16 * eps32 * ||T|| of the FP32 bracket
+    const double margin = 16.0 * 1.1920929e-7 * s_scalar[1] + 1e-300;
+    lo -= margin;
+    hi += margin;
+    for (int round = 0; round < 8; ++round) {
+      const double x = lo + (hi - lo) * (double)(j + 1) / 33.0;
+      const bool hit = sturm_count_f64(d, e2, n, x) >= target;
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      const int f = m ? (__ffs(m) - 1) : 32;
+      const double nlo = (f == 0) ? lo : lo + (hi - lo) * (double)f / 33.0;
+      const double nhi = (f == 32) ? hi : lo + (hi - lo) * (double)(f + 1) / 33.0;
+      lo = nlo;
+      hi = nhi;
+    }
+    if (j == 0) {
+      lohi[which][0] = lo;
+      lohi[which][1] = hi;
+    }
   }
+  __syncthreads();
   if (tid == 0) {
     const double lmin = 0.5 * (lohi[0][0] + lohi[0][1]);
     const double lmax = 0.5 * (lohi[1][0] + lohi[1][1]);

@@ -106,3 +106,40 @@ def test_cpd_error_paths(pkg, ctx):
     # the context is still usable afterwards
     st = pkg.cpd(X, 3, pkg.Options(order=3, max_iter=2), init, ctx=ctx)
     assert np.isfinite(st.f_value)
+
+
+def test_cpd_dimtree_matches_oracle(pkg, ctx):
+    """cpdDimTree (include/CpdDimTree.hpp:317-401) on a 4-way tensor, split {0,1}|{2,3}."""
+    rng = np.random.default_rng(21)
+    dims, R = (20, 18, 16, 14), 5
+    A = [rng.random((I, R)) for I in dims]
+    X = np.einsum("ir,jr,kr,lr->ijkl", *A) + 0.05 * rng.standard_normal(dims)
+    init = [rng.random((I, R)) for I in dims]
+    st = pkg.cpdDimTree(X, R, pkg.Options(order=4, max_iter=12), init, ctx=ctx)
+    ref = oc.cpd_dimtree_als(X, R, oc.Options(order=4, max_iter=12), init)
+    rel_gpu = np.array([t["rel"] for t in st.trace])
+    rel_ref = np.array([s["rel"] for s in ref.trace])
+    assert np.max(np.abs(rel_gpu - rel_ref)) < 1e-4
+    assert oc.congruence(st.factors, ref.factors) >= 0.99
+
+
+@pytest.mark.parametrize("precision", ["f32", "bf16"])
+def test_cpd_dimtree_equals_cpd(pkg, ctx, precision):
+    """The dimension tree is an exact reorganisation: same trajectory as cpd."""
+    rng = np.random.default_rng(22)
+    dims, R = (24, 20, 17, 13), 6
+    A = [rng.random((I, R)) for I in dims]
+    X = np.einsum("ir,jr,kr,lr->ijkl", *A) + 0.05 * rng.standard_normal(dims)
+    init = [rng.random((I, R)) for I in dims]
+    o = pkg.Options(order=4, max_iter=8, precision=precision)
+    a = pkg.cpdDimTree(X, R, o, init, ctx=ctx)
+    b = pkg.cpd(X, R, o, init, ctx=ctx)
+    tol = 1e-4 if precision == "f32" else 2e-3
+    assert abs(a.rel_costFunction - b.rel_costFunction) < tol
+
+
+def test_cpd_dimtree_3way(pkg, ctx):
+    X, _, init = _cfg1_like((30, 26, 22), 4, seed=23)
+    st = pkg.cpdDimTree(X, 4, pkg.Options(order=3, max_iter=10), init, ctx=ctx)
+    ref = oc.cpd_dimtree_als(X, 4, oc.Options(order=3, max_iter=10), init)
+    assert abs(st.rel_costFunction - ref.rel_costFunction) < 1e-4

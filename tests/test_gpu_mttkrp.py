@@ -18,13 +18,15 @@ def _dev(a):
     return torch.tensor(np.ascontiguousarray(a), dtype=torch.float32, device="cuda:0")
 
 
-def _run(pkg, ctx, X, factors, R, mode, precision="f32"):
+def _run(pkg, ctx, X, factors, R, mode, precision="f32", impl="auto"):
+    ctx.set_mttkrp_impl(impl)
     T = pkg.Tensor(ctx, np.asfortranarray(X), precision=precision)
     dev = [_dev(f) for f in factors]
     out = torch.full((X.shape[mode], R), float("nan"), dtype=torch.float32, device="cuda:0")
     pkg.mttkrp(ctx, T, [d.data_ptr() for d in dev], R, mode, out.data_ptr())
     ctx.synchronize()
     T.close()
+    ctx.set_mttkrp_impl("auto")
     return out.cpu().double().numpy()
 
 
@@ -48,13 +50,14 @@ def test_mttkrp_fp32_all_modes(pkg, ctx, dims, R):
 
 
 @pytest.mark.parametrize("dims,R", [((23, 19, 17), 5), ((40, 48, 56), 32), ((12, 10, 9, 8), 20)])
-def test_mttkrp_bf16_storage(pkg, ctx, dims, R):
+def test_mttkrp_bf16_storage_cuda_cores(pkg, ctx, dims, R):
+    """BF16 storage on the CUDA-core kernel: only the tensor is rounded."""
     rng = np.random.default_rng(7 + R)
     X = rng.random(dims)
     f = [rng.random((I, R)) for I in dims]
     Xb = _bf16_round(X)
     for mode in range(len(dims)):
-        got = _run(pkg, ctx, X, f, R, mode, precision="bf16")
+        got = _run(pkg, ctx, X, f, R, mode, precision="bf16", impl="cuda_cores")
         ref_b = oc.mttkrp(f, Xb, mode)
         ref = oc.mttkrp(f, X, mode)
         assert np.linalg.norm(got - ref_b) / np.linalg.norm(ref_b) < 1e-5
@@ -62,12 +65,13 @@ def test_mttkrp_bf16_storage(pkg, ctx, dims, R):
 
 
 def test_mttkrp_reference_contract_500_r40(pkg, ctx):
-    """test/CPD_CUDA/test_batched_mttkrp.cpp: 500^3, R=40, factors in [-1,1],
-    ||M_gpu - M_cpu||_F <= 1e-4 (tensor entries in [-1,1] as Matrix::Random)."""
+    """test/CPD_CUDA/test_batched_mttkrp.cpp:24-27,105-113: 500^3, R=40, true factors
+    Matrix::Random in [-1,1], X = [[A,B,C]] (generateTensor), MTTKRP of X with the same
+    factors, GPU vs CPU ||M_gpu - M_cpu||_F <= 1e-4."""
     rng = np.random.default_rng(500)
     dims = (500, 500, 500)
-    X = rng.uniform(-1, 1, dims)
     f = [rng.uniform(-1, 1, (I, 40)) for I in dims]
+    X = np.einsum("ir,jr,kr->ijk", *f, optimize=True)
     for mode in range(3):
         got = _run(pkg, ctx, X, f, 40, mode)
         ref = oc.mttkrp_einsum(f, X, mode)
