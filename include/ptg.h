@@ -49,6 +49,7 @@ typedef enum {
 
 typedef struct ptg_ctx ptg_ctx;
 typedef struct ptg_tensor ptg_tensor;
+typedef struct ptg_mlp ptg_mlp;
 
 /* Text of the last error raised on this thread ("" if none). */
 const char *ptg_last_error(void);
@@ -82,6 +83,9 @@ typedef struct {
   double mttkrp_ms;           /* summed event time of those contractions */
   double mttkrp_bytes;        /* algorithmic bytes: tensor + factors read, result written */
   double mttkrp_flops;        /* 2 * prod(I) * R per contraction */
+  long long tc_launches;      /* the subset that ran on the tensor cores (tcgen05) */
+  double tc_ms;
+  double tc_bytes;
 } ptg_stats;
 int ptg_ctx_enable_stats(ptg_ctx *ctx, int enable);
 int ptg_ctx_get_stats(ptg_ctx *ctx, ptg_stats *out); /* synchronises the context's stream */
@@ -121,8 +125,13 @@ typedef struct {
   int normalization;
   /* GB300 extensions (Gb300Options): */
   int refine_sweeps; /* FP32 sweeps run on `refine` after the main loop stops (0: none) */
-  int warm_start;    /* 1: MLP warm start for the NNLS rows (needs a trained model) */
+  int warm_start;    /* 1: learned warm start of the NNLS rows with warm_model */
   int cost_every_sweep; /* reserved, must be 1 */
+  ptg_mlp *warm_model;  /* the network (ptg_mlp_create); shared across runs and instances */
+  int warm_log_sweeps;  /* sweeps 1..n log (features, solution) pairs, then the network is
+                           trained warm_train_steps Adam steps and used from sweep n+1;
+                           0: use the network as it is from sweep 1 */
+  int warm_train_steps;
 } ptg_cpd_options;
 
 /* Fill *o with the reference defaults (include/PARTENSOR_basic.hpp:176-218). */
@@ -183,6 +192,67 @@ int ptg_cpd_dimtree(ptg_ctx *ctx, int order, const int64_t *dims, const double *
                     ptg_dtype dtype, int rank, const ptg_cpd_options *opts,
                     const double *const *init_factors, double *const *out_factors,
                     ptg_cpd_result *result, ptg_sweep_trace *trace);
+
+/* ---- Learned warm start (no counterpart in the reference) ------------------------------
+ * A two-hidden-layer ReLU network (128 units) maps the features of an NNLS row -- the
+ * MTTKRP row divided by its norm and eight scale-free summaries of the Hadamard-of-Grams
+ * (Din = R + 8) -- to the solution row scaled by L / ||m_i|| (R outputs).  The Nesterov
+ * solver starts from max(output * ||m_i|| / L, 0) and runs to the reference's own stopping
+ * rule (include/NesterovMNLS.hpp:217-218).  Training and inference run in libptg's kernels. */
+int ptg_mlp_create(ptg_ctx *ctx, int rank, unsigned long long seed, ptg_mlp **out);
+int ptg_mlp_destroy(ptg_mlp *m);
+long long ptg_mlp_num_params(const ptg_mlp *m);
+int ptg_mlp_get_params(ptg_ctx *ctx, const ptg_mlp *m, float *host_out);
+int ptg_mlp_set_params(ptg_ctx *ctx, ptg_mlp *m, const float *host_in);
+/* Y[rows][R] = network(X[rows][R + 8]); device buffers. */
+int ptg_mlp_forward(ptg_ctx *ctx, const ptg_mlp *m, const float *X_dev, long long rows, float *Y_dev);
+/* loss = sum 0.5 ||y - t||^2 / (rows * R) over the data set and its gradient (device, laid out
+ * W1 [H][Din], b1, W2 [H][H], b2, W3 [R][H], b3); rows <= 65536. */
+int ptg_mlp_loss_grad(ptg_ctx *ctx, const ptg_mlp *m, const float *X_dev, const float *T_dev, int rows,
+                      double *loss, float *grad_dev);
+/* `steps` minibatch Adam steps (lr, betas 0.9/0.999) on device data X [rows][R+8], T [rows][R]. */
+int ptg_mlp_train(ptg_ctx *ctx, ptg_mlp *m, const float *X_dev, const float *T_dev, long long rows, int steps,
+                  int batch, float lr, unsigned long long seed, double *final_loss);
+
+/* ---- Sparse tensor completion (GTC) ---------------------------------------------------
+ * partensor::gtc / gtc_stochastic (include/Gtc.hpp:655-757, include/GtcStochastic.hpp:640-742)
+ * with nonnegativity on every mode.  The reference takes an (N+1) x nnz FP64 matrix
+ * Ratings_Base_T (indices stored as doubles, then the value); this ABI takes the same data
+ * as int32 indices idx[k * nnz + e] (mode k of entry e) and FP32 values. */
+typedef struct {
+  int constraints[PTG_MAX_ORDER];   /* PTG_NONNEGATIVITY on every mode */
+  double threshold_error;           /* stop when f / ||x||^2 < threshold (include/Gtc.hpp:449) */
+  int max_nesterov_iter;            /* 20 (include/PARTENSOR_basic.hpp:234) */
+  int max_iter;                     /* outer iterations (full) or epochs (stochastic) */
+  double c_stochastic_perc;         /* sampled fraction per row and inner step */
+  double lambdas[PTG_MAX_ORDER];    /* Tikhonov weights, default 0.01 */
+  int stochastic;                   /* 0: aogtc (include/Gtc.hpp:430-490); 1: aogtc_stochastic */
+  unsigned long long seed;          /* seed of the counter-based pivot sampler */
+} ptg_gtc_options;
+
+void ptg_gtc_default_options(int order, ptg_gtc_options *o);
+
+typedef struct {
+  double frob_tns;          /* sum of squared observed values */
+  double f_value;           /* sum of squared residuals over the observed entries */
+  double rel_costFunction;  /* f_value / frob_tns (not square-rooted, include/Gtc.hpp:449) */
+  int ao_iter;
+  int epochs;
+  double seconds_setup;     /* sorting and layout */
+  double seconds_total;
+} ptg_gtc_result;
+
+/* idx/vals on the host (src_on_device = 0) or the device; init/out factors host FP64
+ * ColMajor I_k x R; trace (optional) receives one record per cost evaluation (max_iter). */
+int ptg_gtc(ptg_ctx *ctx, int order, const int64_t *dims, int64_t nnz, const int32_t *idx, const float *vals,
+            int src_on_device, int rank, const ptg_gtc_options *opts, const double *const *init_factors,
+            double *const *out_factors, ptg_gtc_result *result, ptg_sweep_trace *trace);
+
+/* The mode-n order of the entries (SortRows, include/TensorOperations.hpp:622-666): perm[s]
+ * is the input position of the s-th entry of the mode-n matricisation.  idx and perm on the
+ * device. */
+int ptg_gtc_sort_mode(ptg_ctx *ctx, int order, const int64_t *dims, int64_t nnz, const int32_t *idx_dev,
+                      int mode, uint32_t *perm_out_dev);
 
 #ifdef __cplusplus
 }

@@ -421,6 +421,8 @@ def dimtree_partial(factors: Sequence[np.ndarray], X: np.ndarray, keep: Sequence
 def dimtree_leaf_mttkrp(T: np.ndarray, factors: Sequence[np.ndarray], keep: Sequence[int], mode: int):
     """Leaf step: the node tensor T [I_keep..., R] contracted with the node's other
     factors (TTVs with TensorPartialProduct_R, include/TensorOperations.hpp:196-213)."""
+    if len(keep) == 1:
+        return T
     letters = "abcdefgh"[:len(keep)]
     pos = list(keep).index(mode)
     spec = letters + "z," + ",".join(f"{letters[i]}z" for i, k in enumerate(keep) if k != mode)

@@ -9,4 +9,7 @@ raises.
 """
 from . import _lib  # noqa: F401
 from .cpd import (CONSTANT, NONNEGATIVITY, ORTHOGONALITY, SPARSITY, UNCONSTRAINED, Context,  # noqa: F401
-                  Options, Status, Tensor, cpd, cpd_resident, cpdDimTree, default_context, mttkrp)
+                  Options, Status, Tensor, WarmStartModel, cpd, cpd_resident, cpdDimTree, default_context,
+                  mttkrp)
+from .gtc import SparseOptions, SparseStatus, gtc, gtc_coo, gtc_stochastic  # noqa: F401
+from .gtc import sort_mode as gtc_sort_mode  # noqa: F401

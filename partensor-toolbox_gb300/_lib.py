@@ -23,6 +23,9 @@ EXPORTS = [
     "ptg_tensor_create", "ptg_tensor_destroy", "ptg_tensor_norms",
     "ptg_mttkrp", "ptg_cpd_default_options", "ptg_cpd_als", "ptg_cpd",
     "ptg_cpd_dimtree_als", "ptg_cpd_dimtree",
+    "ptg_gtc_default_options", "ptg_gtc", "ptg_gtc_sort_mode",
+    "ptg_mlp_create", "ptg_mlp_destroy", "ptg_mlp_num_params", "ptg_mlp_get_params", "ptg_mlp_set_params",
+    "ptg_mlp_forward", "ptg_mlp_loss_grad", "ptg_mlp_train",
 ]
 
 
@@ -32,7 +35,8 @@ class CpdOptions(ctypes.Structure):
                 ("max_iter", ctypes.c_int), ("accel_coeff", ctypes.c_int), ("accel_fail", ctypes.c_int),
                 ("acceleration", ctypes.c_int), ("normalization", ctypes.c_int),
                 ("refine_sweeps", ctypes.c_int), ("warm_start", ctypes.c_int),
-                ("cost_every_sweep", ctypes.c_int)]
+                ("cost_every_sweep", ctypes.c_int), ("warm_model", ctypes.c_void_p),
+                ("warm_log_sweeps", ctypes.c_int), ("warm_train_steps", ctypes.c_int)]
 
 
 class CpdResult(ctypes.Structure):
@@ -52,7 +56,21 @@ class SweepTrace(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_longlong), ("mttkrp_launches", ctypes.c_longlong),
                 ("mttkrp_ms", ctypes.c_double), ("mttkrp_bytes", ctypes.c_double),
-                ("mttkrp_flops", ctypes.c_double)]
+                ("mttkrp_flops", ctypes.c_double), ("tc_launches", ctypes.c_longlong),
+                ("tc_ms", ctypes.c_double), ("tc_bytes", ctypes.c_double)]
+
+
+class GtcOptions(ctypes.Structure):
+    _fields_ = [("constraints", ctypes.c_int * MAX_ORDER), ("threshold_error", ctypes.c_double),
+                ("max_nesterov_iter", ctypes.c_int), ("max_iter", ctypes.c_int),
+                ("c_stochastic_perc", ctypes.c_double), ("lambdas", ctypes.c_double * MAX_ORDER),
+                ("stochastic", ctypes.c_int), ("seed", ctypes.c_ulonglong)]
+
+
+class GtcResult(ctypes.Structure):
+    _fields_ = [("frob_tns", ctypes.c_double), ("f_value", ctypes.c_double),
+                ("rel_costFunction", ctypes.c_double), ("ao_iter", ctypes.c_int), ("epochs", ctypes.c_int),
+                ("seconds_setup", ctypes.c_double), ("seconds_total", ctypes.c_double)]
 
 
 class PtgError(RuntimeError):
@@ -93,10 +111,27 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ptg_cpd.argtypes = [vp, ctypes.c_int, i64p, dp, ctypes.c_int, ctypes.c_int,
                             ctypes.POINTER(CpdOptions), dpp, dpp, ctypes.POINTER(CpdResult),
                             ctypes.POINTER(SweepTrace)]
+    lib.ptg_gtc_default_options.argtypes = [ctypes.c_int, ctypes.POINTER(GtcOptions)]
+    lib.ptg_gtc_default_options.restype = None
+    lib.ptg_gtc.argtypes = [vp, ctypes.c_int, i64p, ctypes.c_int64, vp, vp, ctypes.c_int, ctypes.c_int,
+                            ctypes.POINTER(GtcOptions), dpp, dpp, ctypes.POINTER(GtcResult),
+                            ctypes.POINTER(SweepTrace)]
+    lib.ptg_gtc_sort_mode.argtypes = [vp, ctypes.c_int, i64p, ctypes.c_int64, vp, ctypes.c_int, vp]
+    lib.ptg_mlp_create.argtypes = [vp, ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(vp)]
+    lib.ptg_mlp_destroy.argtypes = [vp]
+    lib.ptg_mlp_num_params.argtypes = [vp]
+    lib.ptg_mlp_num_params.restype = ctypes.c_longlong
+    lib.ptg_mlp_get_params.argtypes = [vp, vp, vp]
+    lib.ptg_mlp_set_params.argtypes = [vp, vp, vp]
+    lib.ptg_mlp_forward.argtypes = [vp, vp, vp, ctypes.c_longlong, vp]
+    lib.ptg_mlp_loss_grad.argtypes = [vp, vp, vp, vp, ctypes.c_int, dp, vp]
+    lib.ptg_mlp_train.argtypes = [vp, vp, vp, vp, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                  ctypes.c_ulonglong, dp]
     lib.ptg_cpd_dimtree_als.argtypes = lib.ptg_cpd_als.argtypes
     lib.ptg_cpd_dimtree.argtypes = lib.ptg_cpd.argtypes
     for name in EXPORTS:
-        if name not in ("ptg_last_error", "ptg_version", "ptg_cpd_default_options"):
+        if name not in ("ptg_last_error", "ptg_version", "ptg_cpd_default_options", "ptg_gtc_default_options",
+                        "ptg_mlp_num_params"):
             getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib

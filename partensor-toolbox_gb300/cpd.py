@@ -38,7 +38,10 @@ class Options:
     # GB300 extensions
     precision: str = "f32"        # storage of the tensor in HBM: "f32" or "bf16"
     refine_sweeps: int = 0        # FP32 sweeps after the main loop (bf16 storage only)
-    warm_start: bool = False
+    warm_start: bool = False      # learned warm start of the NNLS rows (needs warm_model)
+    warm_model: object = None     # a WarmStartModel
+    warm_log_sweeps: int = 5      # sweeps that log training pairs before the network is trained
+    warm_train_steps: int = 200
 
     def __post_init__(self):
         if self.constraints is None:
@@ -59,6 +62,9 @@ class Options:
         o.normalization = int(bool(self.normalization))
         o.refine_sweeps = int(self.refine_sweeps)
         o.warm_start = int(bool(self.warm_start))
+        o.warm_model = self.warm_model.handle if self.warm_model is not None else None
+        o.warm_log_sweeps = int(self.warm_log_sweeps)
+        o.warm_train_steps = int(self.warm_train_steps)
         return o
 
 
@@ -107,7 +113,8 @@ class Context:
         s = _lib.Stats()
         check(self._lib.ptg_ctx_get_stats(self.handle, ctypes.byref(s)))
         return dict(launches=s.launches, mttkrp_launches=s.mttkrp_launches, mttkrp_ms=s.mttkrp_ms,
-                    mttkrp_bytes=s.mttkrp_bytes, mttkrp_flops=s.mttkrp_flops)
+                    mttkrp_bytes=s.mttkrp_bytes, mttkrp_flops=s.mttkrp_flops, tc_launches=s.tc_launches,
+                    tc_ms=s.tc_ms, tc_bytes=s.tc_bytes)
 
     def close(self):
         if self.handle:
@@ -175,6 +182,56 @@ class Tensor:
     def close(self):
         if getattr(self, "handle", None):
             self._lib.ptg_tensor_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class WarmStartModel:
+    """The learned NNLS warm start (``ptg_mlp_*``): a 2 x 128 ReLU MLP on the device."""
+
+    def __init__(self, ctx: Context, rank: int, seed: int = 0):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        h = ctypes.c_void_p()
+        check(self._lib.ptg_mlp_create(ctx.handle, int(rank), int(seed), ctypes.byref(h)))
+        self.handle = h
+        self.rank = rank
+        self.n = int(self._lib.ptg_mlp_num_params(h))
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.float32)
+        check(self._lib.ptg_mlp_get_params(self.ctx.handle, self.handle, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(self._lib.ptg_mlp_set_params(self.ctx.handle, self.handle, p.ctypes.data_as(ctypes.c_void_p)))
+
+    def forward(self, X_ptr: int, rows: int, Y_ptr: int):
+        check(self._lib.ptg_mlp_forward(self.ctx.handle, self.handle, ctypes.c_void_p(X_ptr), rows,
+                                        ctypes.c_void_p(Y_ptr)))
+
+    def loss_grad(self, X_ptr: int, T_ptr: int, rows: int, G_ptr: int) -> float:
+        loss = ctypes.c_double()
+        check(self._lib.ptg_mlp_loss_grad(self.ctx.handle, self.handle, ctypes.c_void_p(X_ptr),
+                                          ctypes.c_void_p(T_ptr), rows, ctypes.byref(loss), ctypes.c_void_p(G_ptr)))
+        return loss.value
+
+    def train(self, X_ptr: int, T_ptr: int, rows: int, steps: int, batch: int = 256, lr: float = 1e-3,
+              seed: int = 0) -> float:
+        loss = ctypes.c_double()
+        check(self._lib.ptg_mlp_train(self.ctx.handle, self.handle, ctypes.c_void_p(X_ptr), ctypes.c_void_p(T_ptr),
+                                      rows, steps, batch, lr, seed, ctypes.byref(loss)))
+        return loss.value
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.ptg_mlp_destroy(self.handle)
             self.handle = None
 
     def __del__(self):

@@ -101,6 +101,7 @@ struct Runner {
   int weight = 0;
   bool all_orth = true;
   bool dimtree = false;
+  WarmArgs warm[PTG_MAX_ORDER];   // per mode, for the sweep being run
   std::chrono::steady_clock::time_point t0;
 
   // one ALS sweep over all modes on tensor X; fills f (before acceleration) and per-mode
@@ -130,7 +131,7 @@ struct Runner {
       PTG_CUDA(cudaStreamWaitEvent(S, ctx->ev_join, 0));
       PTG_TRY(launch_nnls_full(ctx, b.M, b.fac[n], b.rows[n], R, b.np, (float)opt->nesterov_delta_1,
                                (float)opt->nesterov_delta_2, b.gram[n], b.dsc + 4 * n,
-                               b.dsc + 4 * n + 1, b.isc + 2 * n, b.isc + 2 * n + 1, S));
+                               b.dsc + 4 * n + 1, b.isc + 2 * n, b.isc + 2 * n + 1, S, warm[n]));
       count_launches(ctx, 1);
     }
     double hd[4 * PTG_MAX_ORDER];
@@ -255,9 +256,50 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
   int ao_iter = 0, ntrace = 0;
   long long inner_total = 0;
   int iters[PTG_MAX_ORDER];
+  // learned warm start: log sweeps 1..n, train, then infer (or infer from sweep 1)
+  ptg_mlp *model = opt.warm_start ? opt.warm_model : nullptr;
+  if (opt.warm_start && !model) return set_error(PTG_ERR_INVALID, "warm_start needs warm_model");
+  if (model && mlp_din(model) != rank + 8) return set_error(PTG_ERR_INVALID, "warm_model rank differs");
+  const int log_sweeps = model ? std::max(0, opt.warm_log_sweeps) : 0;
+  int64_t rows_per_sweep = 0;
+  for (int k = 0; k < N; ++k) rows_per_sweep += X->dims[k];
+  float *logX = nullptr, *logT = nullptr;
+  struct FreeOnExit {
+    void *p = nullptr;
+    ~FreeOnExit() { if (p) cudaFree(p); }
+  } logmem;
+  if (log_sweeps > 0) {
+    const size_t rows = (size_t)log_sweeps * rows_per_sweep;
+    PTG_CUDA(cudaMalloc(&logmem.p, sizeof(float) * rows * (2 * rank + 8)));
+    logX = (float *)logmem.p;
+    logT = logX + rows * (rank + 8);
+  }
+  int64_t logged = 0;
   for (;;) {
     ++ao_iter;
+    for (int n = 0; n < N; ++n) run.warm[n] = WarmArgs();
+    if (model) {
+      if (ao_iter <= log_sweeps) {
+        int64_t off = logged;
+        for (int n = 0; n < N; ++n) {
+          run.warm[n].log_X = logX + off * (rank + 8);
+          run.warm[n].log_T = logT + off * rank;
+          run.warm[n].hidden = mlp_hidden(model);
+          off += X->dims[n];
+        }
+        logged = off;
+      } else {
+        for (int n = 0; n < N; ++n) {
+          run.warm[n].theta = mlp_theta(model);
+          run.warm[n].hidden = mlp_hidden(model);
+        }
+      }
+    }
     PTG_TRY(run.sweep(Xa, frob, &f, iters));
+    if (model && ao_iter == log_sweeps && opt.warm_train_steps > 0) {
+      double loss = 0.0;
+      PTG_TRY(ptg_mlp_train(ctx, model, logX, logT, logged, opt.warm_train_steps, 256, 1e-3f, 1234, &loss));
+    }
     for (int n = 0; n < N; ++n) inner_total += iters[n];
     rel = f / std::sqrt(frob);
     if (opt.normalization && !run.all_orth) {
@@ -311,6 +353,7 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
   if (refine && opt.refine_sweeps > 0) {
     Xa = refine;
     frob = Xa->frob_stored;
+    for (int n = 0; n < N; ++n) run.warm[n] = WarmArgs();
     for (; refined < opt.refine_sweeps; ++refined) {
       PTG_TRY(run.sweep(Xa, frob, &f, iters));
       for (int n = 0; n < N; ++n) inner_total += iters[n];

@@ -60,7 +60,7 @@ int stats_begin(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t *ev) {
   return PTG_OK;
 }
 
-int stats_end(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t ev0, double bytes, double flops) {
+int stats_end(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t ev0, double bytes, double flops, bool tc) {
   if (!ctx->stats.enabled || !ev0) return PTG_OK;
   cudaEvent_t ev1;
   if (ctx->stats.pool.empty()) {
@@ -70,21 +70,26 @@ int stats_end(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t ev0, double bytes, doubl
     ctx->stats.pool.pop_back();
   }
   PTG_CUDA(cudaEventRecord(ev1, s));
-  ctx->stats.pending.emplace_back(ev0, ev1);
+  ctx->stats.pending.push_back({ev0, ev1, tc});
   ctx->stats.mttkrp_launches++;
   ctx->stats.mttkrp_bytes += bytes;
   ctx->stats.mttkrp_flops += flops;
+  if (tc) {
+    ctx->stats.tc_launches++;
+    ctx->stats.tc_bytes += bytes;
+  }
   return PTG_OK;
 }
 
 int stats_resolve(ptg_ctx *ctx) {
   for (auto &pr : ctx->stats.pending) {
-    PTG_CUDA(cudaEventSynchronize(pr.second));
+    PTG_CUDA(cudaEventSynchronize(pr.b));
     float ms = 0.f;
-    PTG_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+    PTG_CUDA(cudaEventElapsedTime(&ms, pr.a, pr.b));
     ctx->stats.mttkrp_ms += ms;
-    ctx->stats.pool.push_back(pr.first);
-    ctx->stats.pool.push_back(pr.second);
+    if (pr.tc) ctx->stats.tc_ms += ms;
+    ctx->stats.pool.push_back(pr.a);
+    ctx->stats.pool.push_back(pr.b);
   }
   ctx->stats.pending.clear();
   return PTG_OK;
@@ -274,6 +279,9 @@ int ptg_ctx_get_stats(ptg_ctx *c, ptg_stats *out) {
   out->mttkrp_ms = c->stats.mttkrp_ms;
   out->mttkrp_bytes = c->stats.mttkrp_bytes;
   out->mttkrp_flops = c->stats.mttkrp_flops;
+  out->tc_launches = c->stats.tc_launches;
+  out->tc_ms = c->stats.tc_ms;
+  out->tc_bytes = c->stats.tc_bytes;
   return PTG_OK;
 }
 
@@ -285,6 +293,8 @@ int ptg_ctx_reset_stats(ptg_ctx *c) {
   const bool en = c->stats.enabled;
   c->stats.launches = c->stats.mttkrp_launches = 0;
   c->stats.mttkrp_ms = c->stats.mttkrp_bytes = c->stats.mttkrp_flops = 0.0;
+  c->stats.tc_launches = 0;
+  c->stats.tc_ms = c->stats.tc_bytes = 0.0;
   c->stats.enabled = en;
   return PTG_OK;
 }

@@ -45,7 +45,13 @@ struct ptg_ctx_stats {
   long long launches = 0;
   long long mttkrp_launches = 0;
   double mttkrp_ms = 0.0, mttkrp_bytes = 0.0, mttkrp_flops = 0.0;
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;   // unresolved event pairs
+  long long tc_launches = 0;
+  double tc_ms = 0.0, tc_bytes = 0.0;
+  struct Pending {
+    cudaEvent_t a, b;
+    bool tc;
+  };
+  std::vector<Pending> pending;   // unresolved event pairs
   std::vector<cudaEvent_t> pool;
 };
 
@@ -120,7 +126,7 @@ int check_device_error(ptg_ctx *ctx);
 // Statistics helpers: count kernel launches; bracket a contraction with events.
 inline void count_launches(ptg_ctx *ctx, int n) { ctx->stats.launches += n; }
 int stats_begin(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t *ev);
-int stats_end(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t ev, double bytes, double flops);
+int stats_end(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t ev, double bytes, double flops, bool tc = false);
 int stats_resolve(ptg_ctx *ctx);   // fold completed event pairs into the sums
 
 // ----------------------------------------------------------------------------------
@@ -133,7 +139,16 @@ struct NnlsParams {
   double Z[64 * 64];   // Hadamard of the Grams (FP64), R x R row-major
   double L, mu, lambda, q;
   float beta[kMaxInner];
+  float feat[8];       // scale-free summaries of Z for the warm-start network
   int status;
+};
+
+// Warm start of the NNLS rows (ptg_mlp.cu): network parameters and the training log.
+struct WarmArgs {
+  const float *theta = nullptr;   // MLP parameters (nullptr: no inference)
+  int hidden = 0;
+  float *log_X = nullptr;         // [rows][R + 8] features  (nullptr: no logging)
+  float *log_T = nullptr;         // [rows][R] targets
 };
 
 int launch_eigen_bounds(const float *const *grams, int order, int mode, int R, NnlsParams *out,
@@ -143,7 +158,8 @@ int launch_eigen_bounds(const float *const *grams, int order, int mode, int R, N
 // the zero-column repair ran.
 int launch_nnls_full(ptg_ctx *ctx, const float *M, float *A, int I, int R, const NnlsParams *np,
                      float delta1, float delta2, float *gram_out, double *inner_MA, double *had_ZG,
-                     int *iters_out, int *repaired_out, cudaStream_t stream);
+                     int *iters_out, int *repaired_out, cudaStream_t stream,
+                     const WarmArgs &warm = WarmArgs());
 size_t gram_scratch_floats(int I, int R);
 int launch_gram(const float *A, int I, int R, float *G, float *part, cudaStream_t stream);
 int launch_normalize(float *const *fac, float *const *gram, const int *rows, int order, int weight,

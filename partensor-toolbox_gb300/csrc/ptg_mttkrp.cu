@@ -460,9 +460,10 @@ int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, 
   cudaEvent_t ev = nullptr;
   PTG_TRY(stats_begin(ctx, stream, &ev));
   int rc;
+  const bool tc = t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 128;
   if (t->dtype == PTG_F32)
     rc = launch_typed<float>(ctx, t, c, R, out, stream);
-  else if (t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 256)
+  else if (tc)
     rc = tc_contraction_launch(ctx, t, c, R, out, stream);
   else if (t->dtype == PTG_BF16)
     rc = launch_typed<__nv_bfloat16>(ctx, t, c, R, out, stream);
@@ -471,7 +472,7 @@ int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, 
   if (rc != PTG_OK) return rc;
   double numel = 1.0;
   for (int k = 0; k < t->order; ++k) numel *= (double)t->dims[k];
-  return stats_end(ctx, stream, ev, contraction_bytes(t, c, R), 2.0 * numel * R);
+  return stats_end(ctx, stream, ev, contraction_bytes(t, c, R), 2.0 * numel * R, tc);
 }
 
 }  // namespace ptg

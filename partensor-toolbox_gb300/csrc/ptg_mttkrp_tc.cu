@@ -426,7 +426,7 @@ size_t tc_smem_bytes(int N) {
 int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                           cudaStream_t stream) {
   if (t->dtype != PTG_BF16) return set_error(PTG_ERR_INVALID, "internal: tcgen05 path needs BF16 storage");
-  if (R > 256) return set_error(PTG_ERR_UNSUPPORTED, "tcgen05 MTTKRP: rank > 256");
+  if (R > 128) return set_error(PTG_ERR_UNSUPPORTED, "tcgen05 MTTKRP: rank > 128");
   EncodeTiledFn enc = encode_fn();
   if (!enc) return set_error(PTG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
   const bool mmajor = (c.P == 1);

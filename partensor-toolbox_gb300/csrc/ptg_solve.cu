@@ -103,14 +103,19 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
   }
   __syncthreads();
 
+  // Block sum: FP64 partials reduced by one thread and broadcast (GB300 executes FP64 at a
+  // small fraction of the FP32 rate, so no FP64 work is repeated across threads).
   auto block_sum = [&](double x) -> double {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if ((tid & 31) == 0) red[tid >> 5] = x;
     __syncthreads();
-    double s = 0.0;
-    for (int i = 0; i < kEigThreads / 32; ++i) s += red[i];
+    if (tid == 0) {
+      double s = 0.0;
+      for (int i = 0; i < kEigThreads / 32; ++i) s += red[i];
+      s_scalar[2] = s;
+    }
     __syncthreads();
-    return s;
+    return s_scalar[2];
   };
 
   // ---- Householder tridiagonalisation (A symmetric, row-major n x n) ----
@@ -129,11 +134,16 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
       __syncthreads();
       continue;
     }
-    const double alpha = (x0 >= 0.0 ? -1.0 : 1.0) * sqrt(x0 * x0 + sigma);
+    if (tid == 0) {   // the step's scalars, once
+      const double al = (x0 >= 0.0 ? -1.0 : 1.0) * sqrt(x0 * x0 + sigma);
+      s_scalar[0] = al;
+      s_scalar[3] = 2.0 / ((x0 - al) * (x0 - al) + sigma);
+    }
+    __syncthreads();
+    const double alpha = s_scalar[0];
+    const double beta = s_scalar[3];
     for (int i = tid; i < m; i += blockDim.x) v[i] = (i == 0) ? (x0 - alpha) : A[(k + 1 + i) * n + k];
     __syncthreads();
-    const double vtv = (x0 - alpha) * (x0 - alpha) + sigma;
-    const double beta = 2.0 / vtv;
     // p = beta * A_sub v   (rows of the trailing block split over the threads)
     for (int i = tid; i < m; i += blockDim.x) {
       const double *row = &A[(k + 1 + i) * n + (k + 1)];
@@ -224,6 +234,23 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
     double L = fmax(fabs(lmax), fabs(lmin));
     double mu = fabs(lmin);
     if (n == 1) L = mu = fabs(d[0]);
+    {   // scale-free summaries of Z for the warm-start network
+      double dsum = 0.0, dmin = 1e300, dmax = -1e300;
+      for (int i = 0; i < n; ++i) {
+        const double z = out->Z[i * n + i];
+        dsum += z;
+        dmin = fmin(dmin, z);
+        dmax = fmax(dmax, z);
+      }
+      const double Ls = L > 0.0 ? L : 1.0;
+      out->feat[0] = (float)(log10(Ls / fmax(mu, 1e-300)) / 6.0);
+      out->feat[1] = (float)(mu / Ls);
+      out->feat[2] = (float)(dsum / n / Ls);
+      out->feat[3] = (float)(dmin / Ls);
+      out->feat[4] = (float)(dmax / Ls);
+      out->feat[6] = (float)n / 64.0f;
+      out->feat[7] = 1.0f;
+    }
     // GLambda, include/NesterovMNLS.hpp:75-91
     double q = mu / L, lam;
     if (1.0 / q > 1e6) lam = 10.0 * mu;
@@ -236,11 +263,15 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
     out->mu = mu;
     out->lambda = lam;
     out->q = q;
-    double alpha = 1.0;
-    for (int it = 0; it < kMaxInner; ++it) {   // UpdateAlpha, :103-113
-      const double b = alpha * alpha - q, c = -alpha * alpha;
-      const double na = (-b + sqrt(b * b - 4.0 * c)) / 2.0;
-      out->beta[it] = (float)(alpha * (1.0 - alpha) / (alpha * alpha + na));
+    out->feat[5] = (float)(lam / L);
+    // UpdateAlpha (:103-113) and beta (:226): the sequence is consumed in FP32 by the
+    // solver, so it is generated in FP32 (a serial FP64 chain would dominate the kernel)
+    float alpha = 1.0f;
+    const float qf = (float)q;
+    for (int it = 0; it < kMaxInner; ++it) {
+      const float b = alpha * alpha - qf, c = -alpha * alpha;
+      const float na = (-b + sqrtf(b * b - 4.0f * c)) * 0.5f;
+      out->beta[it] = alpha * (1.0f - alpha) / (alpha * alpha + na);
       alpha = na;
     }
     out->status = (isfinite(L) && isfinite(mu)) ? 0 : PTG_ERR_NUMERIC;
@@ -265,6 +296,11 @@ struct NnlsArgs {
   double *had_ZG;        // sum(Z .* G_new) (FP64)
   int *iters_out;
   int *repaired_out;
+  // learned warm start (optional)
+  const float *theta;    // MLP parameters: W1 [H][Din], b1, W2 [H][H], b2, W3 [R][H], b3
+  int hidden;
+  float *log_X;          // [I][R + 8] features of each row (optional)
+  float *log_T;          // [I][R] solution scaled by L / ||m_i|| (optional)
 };
 
 template <int RB, int ROWS>
@@ -280,9 +316,10 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   float *As = Zt + R * R;                           // (kNnlsWarps*ROWS) x R
   float *Gp = As + kNnlsWarps * ROWS * R;           // R*R  (this CTA's partial Gram)
   float *colsum = Gp + R * R;                       // R
-  double *slots = reinterpret_cast<double *>(colsum + ((R + 1) & ~1));  // [2][2] stop test
-  double *wred = slots + 4;                         // kNnlsWarps * 2
-  double *ma = wred + 2 * kNnlsWarps;               // 1: this CTA's <M, A>
+  float *slots = colsum + ((R + 1) & ~1);          // [2][2] stop test (max |g.y|, min g)
+  float *wred = slots + 4;                          // kNnlsWarps * 2
+  double *wredd = reinterpret_cast<double *>(wred + 2 * kNnlsWarps);   // kNnlsWarps
+  double *ma = wredd + kNnlsWarps;                  // 1: this CTA's <M, A>
   int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired
 
   const NnlsParams *np = a.np;
@@ -315,6 +352,87 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
       Ac[j][b] = a0;
       Y[j][b] = a0;
       Wt[j][b] = m + lam * a0;                      // W~ = W + lambda A0   (:206)
+    }
+  }
+  // ---- learned warm start: features of each row, network inference, logging ----
+  float rscale[ROWS];
+  if (a.theta || a.log_X) {
+    const int Din = R + 8, H = a.hidden;
+    const float Lf = (float)np->L;
+    float feat[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) feat[t] = np->feat[t];
+#pragma unroll
+    for (int j = 0; j < ROWS; ++j) {
+      const int i = gw + j * stride;
+      float m[RB];
+      float s2 = 0.0f;
+#pragma unroll
+      for (int b = 0; b < RB; ++b) {
+        const int c = lane + 32 * b;
+        m[b] = (i < I && colok[b]) ? a.M[(size_t)i * R + c] : 0.0f;
+        s2 = fmaf(m[b], m[b], s2);
+      }
+      for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      const float sc = sqrtf(s2) + 1e-30f;
+      rscale[j] = sc;
+      float x[RB];
+#pragma unroll
+      for (int b = 0; b < RB; ++b) x[b] = m[b] / sc;
+      if (a.log_X && i < I) {
+#pragma unroll
+        for (int b = 0; b < RB; ++b)
+          if (colok[b]) a.log_X[(size_t)i * Din + lane + 32 * b] = x[b];
+        if (lane < 8) a.log_X[(size_t)i * Din + R + lane] = feat[lane];
+      }
+      if (a.theta && i < I) {   // uniform per warp: i depends on the warp only
+        const float *W1 = a.theta, *b1 = W1 + (size_t)H * Din, *W2 = b1 + H, *b2 = W2 + (size_t)H * H;
+        const float *W3 = b2 + H, *b3 = W3 + (size_t)R * H;
+        float h1[4], h2[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) h1[q] = (lane + 32 * q < H) ? __ldg(b1 + lane + 32 * q) : 0.0f;
+        for (int jj = 0; jj < R; ++jj) {
+          const float xj = __shfl_sync(0xffffffffu, (jj >> 5) == 0 ? x[0] : x[RB - 1], jj & 31);
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (lane + 32 * q < H) h1[q] = fmaf(__ldg(W1 + (size_t)(lane + 32 * q) * Din + jj), xj, h1[q]);
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (lane + 32 * q < H) h1[q] = fmaf(__ldg(W1 + (size_t)(lane + 32 * q) * Din + R + t), feat[t], h1[q]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          h1[q] = fmaxf(h1[q], 0.0f);
+          h2[q] = (lane + 32 * q < H) ? __ldg(b2 + lane + 32 * q) : 0.0f;
+        }
+        for (int v = 0; v < H; ++v) {
+          const int qv = v >> 5;
+          const float hv = __shfl_sync(0xffffffffu, qv == 0 ? h1[0] : qv == 1 ? h1[1] : qv == 2 ? h1[2] : h1[3], v & 31);
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (lane + 32 * q < H) h2[q] = fmaf(__ldg(W2 + (size_t)(lane + 32 * q) * H + v), hv, h2[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) h2[q] = fmaxf(h2[q], 0.0f);
+        float y[RB];
+#pragma unroll
+        for (int b = 0; b < RB; ++b) y[b] = colok[b] ? __ldg(b3 + lane + 32 * b) : 0.0f;
+        for (int u = 0; u < H; ++u) {
+          const int qu = u >> 5;
+          const float hu = __shfl_sync(0xffffffffu, qu == 0 ? h2[0] : qu == 1 ? h2[1] : qu == 2 ? h2[2] : h2[3], u & 31);
+#pragma unroll
+          for (int b = 0; b < RB; ++b)
+            if (colok[b]) y[b] = fmaf(__ldg(W3 + (size_t)(lane + 32 * b) * H + u), hu, y[b]);
+        }
+#pragma unroll
+        for (int b = 0; b < RB; ++b) {
+          const float st = colok[b] ? fmaxf(y[b] * sc / Lf, 0.0f) : 0.0f;
+          Y[j][b] = st;
+          Ac[j][b] = st;
+        }
+      }
     }
   }
   __syncthreads();
@@ -359,28 +477,31 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
       wred[2 * warp + 1] = mn;
     }
     __syncthreads();
-    if (tid == 0) {
-      double M1 = 0.0, M2 = INFINITY;
-      for (int w = 0; w < kNnlsWarps; ++w) {
-        M1 = fmax(M1, wred[2 * w]);
-        M2 = fmin(M2, wred[2 * w + 1]);
+    if (warp == 0) {   // max/min are exact in FP32, so the reduction order does not matter
+      float M1 = lane < kNnlsWarps ? wred[2 * lane] : 0.0f;
+      float M2 = lane < kNnlsWarps ? wred[2 * lane + 1] : INFINITY;
+      for (int o = 8; o > 0; o >>= 1) {
+        M1 = fmaxf(M1, __shfl_xor_sync(0xffffffffu, M1, o));
+        M2 = fminf(M2, __shfl_xor_sync(0xffffffffu, M2, o));
       }
-      slots[2 * (it & 1)] = M1;
-      slots[2 * (it & 1) + 1] = M2;
+      if (lane == 0) {
+        slots[2 * (it & 1)] = M1;
+        slots[2 * (it & 1) + 1] = M2;
+      }
     }
     cluster.sync();
-    double gmx = 0.0, gmn = INFINITY;
+    float gmx = 0.0f, gmn = INFINITY;
     if (lane < CS) {
-      const double *rs = cluster.map_shared_rank(slots, lane);
+      const float *rs = cluster.map_shared_rank(slots, lane);
       gmx = rs[2 * (it & 1)];
       gmn = rs[2 * (it & 1) + 1];
     }
     for (int o = 16; o > 0; o >>= 1) {
-      gmx = fmax(gmx, __shfl_xor_sync(0xffffffffu, gmx, o));
-      gmn = fmin(gmn, __shfl_xor_sync(0xffffffffu, gmn, o));
+      gmx = fmaxf(gmx, __shfl_xor_sync(0xffffffffu, gmx, o));
+      gmn = fminf(gmn, __shfl_xor_sync(0xffffffffu, gmn, o));
     }
     // stop test of include/NesterovMNLS.hpp:217-218
-    if ((gmx <= (double)a.delta1 && gmn >= -(double)a.delta2) || it >= kMaxInner) break;
+    if ((gmx <= a.delta1 && gmn >= -a.delta2) || it >= kMaxInner) break;
     const float beta = np->beta[it];
 #pragma unroll
     for (int j = 0; j < ROWS; ++j)
@@ -448,11 +569,15 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
 #pragma unroll
     for (int b = 0; b < RB; ++b) {
       const int c = lane + 32 * b;
-      if (i < I && colok[b]) a.A[(size_t)i * R + c] = As[(warp * ROWS + j) * R + c];
+      if (i < I && colok[b]) {
+        const float v = As[(warp * ROWS + j) * R + c];
+        a.A[(size_t)i * R + c] = v;
+        if (a.log_T) a.log_T[(size_t)i * R + c] = v * (float)np->L / rscale[j];
+      }
     }
   }
   for (int o = 16; o > 0; o >>= 1) ma_part += __shfl_xor_sync(0xffffffffu, ma_part, o);
-  if (lane == 0) wred[warp] = ma_part;
+  if (lane == 0) wredd[warp] = ma_part;
   // partial Gram of this CTA's rows
   const int nrows = kNnlsWarps * ROWS;
   for (int idx = tid; idx < R * R; idx += blockDim.x) {
@@ -464,7 +589,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   __syncthreads();
   if (tid == 0) {
     double s = 0.0;
-    for (int w = 0; w < kNnlsWarps; ++w) s += wred[w];
+    for (int w = 0; w < kNnlsWarps; ++w) s += wredd[w];
     ma[0] = s;
   }
   cluster.sync();
@@ -495,8 +620,8 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
 
 template <int RB, int ROWS>
 size_t nnls_smem_bytes(int R) {
-  return sizeof(float) * (2 * R * R + kNnlsWarps * ROWS * R + ((R + 1) & ~1)) +
-         sizeof(double) * (4 + 2 * kNnlsWarps + 2) + 16;
+  return sizeof(float) * (2 * R * R + kNnlsWarps * ROWS * R + ((R + 1) & ~1) + 4 + 2 * kNnlsWarps) +
+         sizeof(double) * (kNnlsWarps + 2) + 16;
 }
 
 template <int RB, int ROWS>
@@ -593,9 +718,10 @@ int launch_eigen_bounds(const float *const *grams, int order, int mode, int R, N
 
 int launch_nnls_full(ptg_ctx *ctx, const float *M, float *A, int I, int R, const NnlsParams *np,
                      float delta1, float delta2, float *gram_out, double *inner_MA, double *had_ZG,
-                     int *iters_out, int *repaired_out, cudaStream_t stream) {
+                     int *iters_out, int *repaired_out, cudaStream_t stream, const WarmArgs &warm) {
   if (R > kMaxR) return set_error(PTG_ERR_UNSUPPORTED, "rank > 64 is not supported by the NNLS path");
-  NnlsArgs args{M, A, I, R, np, delta1, delta2, gram_out, inner_MA, had_ZG, iters_out, repaired_out};
+  NnlsArgs args{M, A, I, R, np, delta1, delta2, gram_out, inner_MA, had_ZG, iters_out, repaired_out,
+                warm.theta, warm.hidden, warm.log_X, warm.log_T};
   const int cs = nnls_cluster_size(ctx);
   const int cap = cs * kNnlsWarps;   // rows per register slot
   const int rows = (I + cap - 1) / cap;

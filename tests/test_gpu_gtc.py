@@ -1,0 +1,88 @@
+"""GPU parity of sparse tensor completion (ptg_gtc) against the FP64 oracle (oracle/gtc.py).
+
+The index sort is bit-exact (the permutation must equal the oracle's SortRows order).  The
+solves run in FP32 on the GPU: the relative cost per iteration must follow the oracle
+within 2e-4 absolute (rel is a ratio of squared norms ~1e-2 here) and the factors must be
+congruent >= 0.99."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import cpd as oc
+from oracle import gtc as og
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("dims,nnz", [((60, 50, 40), 20000), ((31, 17, 23, 9), 15000), ((300, 7, 5), 3000)])
+def test_sort_is_bitexact(pkg, ctx, dims, nnz):
+    idx, vals, _ = og.make_gtc_problem(dims, nnz, 3, seed=nnz)
+    d_idx = torch.tensor(idx.astype(np.int32), device="cuda").contiguous()
+    for mode in range(len(dims)):
+        perm = torch.zeros(nnz, dtype=torch.int32, device="cuda")
+        pkg.gtc_sort_mode(ctx, d_idx.data_ptr(), list(dims), nnz, mode, perm.data_ptr())
+        got = perm.cpu().numpy().astype(np.int64)
+        ref = og.matricize(idx, vals, dims, mode).perm
+        assert np.array_equal(got, ref), mode
+
+
+def _problem(dims, nnz, R, seed):
+    idx, vals, A = og.make_gtc_problem(dims, nnz, R, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    init = [rng.random((I, R)) for I in dims]
+    return idx, vals, init
+
+
+def test_gtc_matches_oracle(pkg, ctx):
+    dims, R = (60, 50, 40), 4
+    idx, vals, init = _problem(dims, 20000, R, 5)
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=8, lambdas=[1e-3] * 3,
+                          factorsInit=init)
+    st = pkg.gtc_coo(idx, vals, o, ctx=ctx)
+    ref = og.gtc(idx, vals, dims, R, og.SparseOptions(order=3, max_iter=8, lambdas=[1e-3] * 3), init)
+    rel_gpu = np.array([t["rel"] for t in st.trace])
+    rel_ref = np.array([t["rel"] for t in ref.trace])
+    assert len(rel_gpu) == len(rel_ref) == 8
+    assert np.max(np.abs(rel_gpu - rel_ref)) < 2e-4, (rel_gpu, rel_ref)
+    assert oc.congruence(st.factors, ref.factors) >= 0.99
+    # the reported cost is the cost of the returned factors
+    f = og.gtc_cost(st.factors, idx, vals)
+    assert f == pytest.approx(st.f_value, rel=1e-3)
+
+
+def test_gtc_ratings_base_interface(pkg, ctx):
+    dims, R = (30, 25, 20), 3
+    idx, vals, init = _problem(dims, 4000, R, 7)
+    ratings = np.vstack([idx.astype(np.float64), vals[None, :]])     # (N+1) x nnz
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=3, factorsInit=init)
+    a = pkg.gtc(ratings, o, ctx=ctx)
+    b = pkg.gtc_coo(idx, vals, o, ctx=ctx)
+    for k in range(3):
+        assert np.array_equal(a.factors[k], b.factors[k])
+
+
+def test_gtc_stochastic_matches_oracle(pkg, ctx):
+    dims, R = (40, 30, 20), 3
+    idx, vals, init = _problem(dims, 12000, R, 9)
+    c = 0.1
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=2, c_stochastic_perc=c,
+                          lambdas=[1e-3] * 3, seed=11, factorsInit=init)
+    st = pkg.gtc_coo(idx, vals, o, stochastic=True, ctx=ctx)
+    ref = og.gtc_stochastic(idx, vals, dims, R,
+                            og.SparseOptions(order=3, max_iter=2, c_stochastic_perc=c, lambdas=[1e-3] * 3,
+                                             seed=11), init)
+    assert st.ao_iter == ref.ao_iter
+    rel_gpu = np.array([t["rel"] for t in st.trace])
+    rel_ref = np.array([t["rel"] for t in ref.trace])
+    assert np.max(np.abs(rel_gpu - rel_ref)) < 1e-3, (rel_gpu, rel_ref)
+
+
+def test_gtc_rejects_duplicates(pkg, ctx):
+    dims, R = (10, 9, 8), 2
+    idx, vals, init = _problem(dims, 200, R, 3)
+    idx = np.concatenate([idx, idx[:, :1]], axis=1)
+    vals = np.concatenate([vals, vals[:1]])
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=2, factorsInit=init)
+    with pytest.raises(pkg._lib.PtgError) as e:
+        pkg.gtc_coo(idx, vals, o, ctx=ctx)
+    assert e.value.code == pkg._lib.PTG_ERR_INVALID
