@@ -110,6 +110,11 @@ Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors,
 int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                        cudaStream_t stream);
 
+// Warm-start network accessors (ptg_mlp.cu).
+const float *mlp_theta(const ptg_mlp *m);
+int mlp_din(const ptg_mlp *m);
+int mlp_hidden(const ptg_mlp *m);
+
 // Dimension tree (ptg_dimtree.cu): split point, node contraction, node size, leaf MTTKRP.
 int dimtree_split(int order);
 Contraction node_contraction(const ptg_tensor *t, const float *const *factors, bool left_node);
