@@ -111,6 +111,27 @@ int ptg_tensor_norms(const ptg_tensor *t, double *frob64, double *frob_stored);
 int ptg_mttkrp(ptg_ctx *ctx, const ptg_tensor *X, const float *const *factors, int rank, int mode,
                float *out);
 
+/* MTTKRP that allocates no device memory.  This entry point has no counterpart in the
+ * reference.  It is for callers that may not call cudaMalloc when they need the product:
+ * applications whose allocator owns all of HBM, code that must not synchronise the device
+ * (cudaMalloc and cudaFree can), latency-bound loops.  It computes what ptg_mttkrp computes,
+ * on CUDA cores, from caller-owned buffers only, with its split-K partials in a fixed 8 MiB
+ * block of device memory that the library image carries (held on every GPU that loads the
+ * library until the process exits).
+ *   X        device FP32 tensor, ColMajor with mode-0 stride ld0: element (i0, i1, ...) at
+ *            i0 + ld0*(i1 + I1*(i2 + ...)); ld0 >= dims[0], ld0 % 8 == 0, X 16-byte aligned;
+ *            the ld0 - dims[0] padding entries of each fibre must be finite (zeros are best)
+ *   factors  device row-major FP32 [I_k][rank] (factors[mode] is not read)
+ *   out      device row-major FP32 [I_mode][rank]
+ *   stream   cudaStream_t (NULL: the legacy default stream)
+ * Limit: I_mode x R_pad <= 2,097,152 floats (ld0 for mode 0; R_pad = rank rounded up to 16,
+ * 32, 64 or 128); larger calls return PTG_ERR_UNSUPPORTED.  The first call on a device looks
+ * up the block's address on that device: make it before any stream capture.  Calls share the
+ * block, so two calls that overlap on the GPU race; the block keeps the last call's data and
+ * nothing in it needs clearing. */
+int ptg_mttkrp_noalloc(const float *X, int order, const int64_t *dims, int64_t ld0,
+                       const float *const *factors, int rank, int mode, float *out, void *stream);
+
 /* Options of one CPD-ALS run: the fields of partensor::Options
  * (include/PARTENSOR_basic.hpp:283-336) that the ALS loop reads, plus GB300 knobs. */
 typedef struct {

@@ -22,7 +22,7 @@ EXPORTS = [
     "ptg_ctx_synchronize", "ptg_ctx_set_option", "ptg_ctx_enable_stats", "ptg_ctx_get_stats", "ptg_ctx_reset_stats",
     "ptg_tensor_create", "ptg_tensor_destroy", "ptg_tensor_norms",
     "ptg_mttkrp", "ptg_cpd_default_options", "ptg_cpd_als", "ptg_cpd",
-    "ptg_cpd_dimtree_als", "ptg_cpd_dimtree",
+    "ptg_cpd_dimtree_als", "ptg_cpd_dimtree", "ptg_mttkrp_noalloc",
     "ptg_gtc_default_options", "ptg_gtc", "ptg_gtc_sort_mode",
     "ptg_mlp_create", "ptg_mlp_destroy", "ptg_mlp_num_params", "ptg_mlp_get_params", "ptg_mlp_set_params",
     "ptg_mlp_forward", "ptg_mlp_loss_grad", "ptg_mlp_train",
@@ -111,6 +111,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ptg_cpd.argtypes = [vp, ctypes.c_int, i64p, dp, ctypes.c_int, ctypes.c_int,
                             ctypes.POINTER(CpdOptions), dpp, dpp, ctypes.POINTER(CpdResult),
                             ctypes.POINTER(SweepTrace)]
+    lib.ptg_mttkrp_noalloc.argtypes = [vp, ctypes.c_int, i64p, ctypes.c_int64, ctypes.POINTER(vp),
+                                       ctypes.c_int, ctypes.c_int, vp, vp]
     lib.ptg_gtc_default_options.argtypes = [ctypes.c_int, ctypes.POINTER(GtcOptions)]
     lib.ptg_gtc_default_options.restype = None
     lib.ptg_gtc.argtypes = [vp, ctypes.c_int, i64p, ctypes.c_int64, vp, vp, ctypes.c_int, ctypes.c_int,

@@ -110,6 +110,12 @@ Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors,
 int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                        cudaStream_t stream);
 
+// CUDA-core MTTKRP on FP32 storage with a caller-owned split-K scratch block of cap_floats
+// floats (ptg_noalloc.cu); needs at least simt_fixed_scratch_floats_needed() floats.
+size_t simt_fixed_scratch_floats_needed(const Contraction &c, int R);
+int simt_mttkrp_fixed_scratch(const ptg_tensor *t, const Contraction &c, int R, float *out, cudaStream_t stream,
+                              int sm_count, float *scratch, size_t cap_floats);
+
 // Warm-start network accessors (ptg_mlp.cu).
 const float *mlp_theta(const ptg_mlp *m);
 int mlp_din(const ptg_mlp *m);

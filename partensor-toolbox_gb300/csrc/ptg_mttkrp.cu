@@ -415,6 +415,90 @@ int launch_typed(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R,
 
 }  // namespace
 
+namespace {
+
+// Launch planning for a caller-owned scratch block of cap_floats floats: the same kernels as
+// launch_cfg, with the K-split count capped so the partials fit, and the partials always
+// used (even with one split) so the block is the only device memory touched besides the
+// inputs and the output.
+template <int BN>
+int launch_cfg_fixed(const ptg_tensor *t, const Contraction &c, int R, int col0, float *out,
+                     cudaStream_t stream, int sm_count, float *scratch, size_t cap_floats) {
+  using Cf = Cfg<BN>;
+  const bool mmajor = (c.P == 1);
+  SimtParams prm{};
+  prm.X = t->data;
+  prm.P = c.P;
+  prm.Q = c.Q;
+  prm.S = c.S;
+  prm.before = to_dev(c.before);
+  prm.after = to_dev(c.after);
+  prm.R = R;
+  prm.col0 = col0;
+  prm.out = out;
+  prm.q_write = c.q_write;
+  prm.ldo = R;
+  if (mmajor) {
+    prm.pblocks = 1;
+    prm.ktiles_total = (c.S + BK - 1) / BK;
+  } else {
+    prm.pblocks = (c.P + BK - 1) / BK;
+    prm.ktiles_total = c.S * prm.pblocks;
+  }
+  const int64_t slab = c.Q * BN;   // floats of one split's partial block
+  const int64_t cap_splits = (int64_t)(cap_floats / (size_t)slab);
+  if (cap_splits < 1) return set_error(PTG_ERR_UNSUPPORTED, "internal: scratch block too small");
+  const int64_t mtiles = (c.Q + Cf::BM - 1) / Cf::BM;
+  const int64_t target = (int64_t)sm_count * 4;
+  int64_t nsplit = std::max<int64_t>(1, (target + mtiles - 1) / mtiles);
+  nsplit = std::min<int64_t>(nsplit, cap_splits);
+  nsplit = std::min<int64_t>(nsplit, prm.ktiles_total);
+  nsplit = std::max<int64_t>(nsplit, 1);
+  prm.ktiles_per_split = (prm.ktiles_total + nsplit - 1) / nsplit;
+  nsplit = (prm.ktiles_total + prm.ktiles_per_split - 1) / prm.ktiles_per_split;
+  // nsplit >= 2 makes the kernel write partials; a single split is forced through them too
+  prm.nsplit = (int)std::max<int64_t>(nsplit, 2);
+  prm.partial = scratch;
+  dim3 grid((unsigned)mtiles, (unsigned)nsplit);
+  const size_t smem = simt_smem_bytes<BN>(mmajor);
+  if (mmajor) {
+    PTG_CUDA(cudaFuncSetAttribute(mttkrp_simt_kernel<float, BN, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    mttkrp_simt_kernel<float, BN, true><<<grid, kThreads, smem, stream>>>(prm);
+  } else {
+    PTG_CUDA(cudaFuncSetAttribute(mttkrp_simt_kernel<float, BN, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    mttkrp_simt_kernel<float, BN, false><<<grid, kThreads, smem, stream>>>(prm);
+  }
+  PTG_CUDA(cudaGetLastError());
+  const int64_t n = c.q_write * BN;
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count * 8);
+  splitk_reduce_kernel<<<std::max(blocks, 1), 256, 0, stream>>>(scratch, (int)nsplit, c.Q, BN, c.q_write, R,
+                                                                col0, R, out);
+  PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
+}
+
+}  // namespace
+
+size_t simt_fixed_scratch_floats_needed(const Contraction &c, int R) {
+  const int bn = R <= 16 ? 16 : R <= 32 ? 32 : R <= 64 ? 64 : 128;
+  return (size_t)c.Q * bn;
+}
+
+int simt_mttkrp_fixed_scratch(const ptg_tensor *t, const Contraction &c, int R, float *out, cudaStream_t stream,
+                              int sm_count, float *scratch, size_t cap_floats) {
+  if (t->dtype != PTG_F32) return set_error(PTG_ERR_UNSUPPORTED, "internal: FP32 storage expected");
+  if (c.P > 0xffffffffLL || c.S > 0xffffffffLL)
+    return set_error(PTG_ERR_UNSUPPORTED, "contraction extent exceeds 2^32");
+  if (R <= 16) return launch_cfg_fixed<16>(t, c, R, 0, out, stream, sm_count, scratch, cap_floats);
+  if (R <= 32) return launch_cfg_fixed<32>(t, c, R, 0, out, stream, sm_count, scratch, cap_floats);
+  if (R <= 64) return launch_cfg_fixed<64>(t, c, R, 0, out, stream, sm_count, scratch, cap_floats);
+  for (int c0 = 0; c0 < R; c0 += 128)
+    PTG_TRY(launch_cfg_fixed<128>(t, c, R, c0, out, stream, sm_count, scratch, cap_floats));
+  return PTG_OK;
+}
+
 Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors, int mode) {
   Contraction c;
   const int N = t->order;
