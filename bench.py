@@ -186,7 +186,7 @@ def run_ours(args):
     ge = __import__("__graft_entry__")
     pkg = ge.load_package()
     from partensor_toolbox_gb300 import datagen as dg
-    dims, R = DIMS if not args.small else [200, 200, 200], RANK
+    dims, R = (args.dims or DIMS) if not args.small else [200, 200, 200], RANK
     p = dg.make_cpd_problem(dims, R, seed=SEED, init_seed=INIT_SEED, snr_db=SNR_DB, equalize_columns=True,
                             device="cuda")
     target = p.noise_rel + 1e-3
@@ -328,6 +328,7 @@ def main():
     ap.add_argument("--steps-e2e", type=int, default=2)
     ap.add_argument("--max-iter", type=int, default=200)
     ap.add_argument("--small", action="store_true", help="200^3 smoke configuration")
+    ap.add_argument("--dims", type=int, nargs=3, default=None, help="override the tensor shape (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--warmup-ref", type=int, default=0)

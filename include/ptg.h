@@ -214,6 +214,29 @@ int ptg_cpd_dimtree(ptg_ctx *ctx, int order, const int64_t *dims, const double *
                     const double *const *init_factors, double *const *out_factors,
                     ptg_cpd_result *result, ptg_sweep_trace *trace);
 
+/* ---- Many small CPDs in one call ------------------------------------------------------
+ * Solves n independent nonnegative CPD-ALS problems of the same order (ranks and dims may
+ * differ per instance) with the semantics of ptg_cpd on an FP32 tensor, each instance
+ * stopping on its own test.  The reference has no batched entry point: a caller loops over
+ * partensor::cpd(tnsX, R, options, factorsInit) (include/Cpd.hpp:534-577), one problem at a
+ * time; this call replaces that loop.  Every ALS phase is one launch for all unfinished
+ * instances and each sweep replays a captured CUDA graph.  Limits: order in [3, 8], every
+ * mode PTG_NONNEGATIVITY, rank <= 32, dims <= 4096, and 3 * rows * rank FP32 values of each
+ * factor within one CTA's shared memory.  results[i].seconds_total is the wall time from the
+ * call's start until instance i's stop test passed; converge_seconds (optional, n entries)
+ * the same time counted from the start of the ALS loop, once every tensor is resident. */
+typedef struct ptg_cpd_instance {
+  int order;
+  int64_t dims[PTG_MAX_ORDER];
+  const double *tensor;                 /* host FP64, ColMajor (mode 0 fastest) */
+  int rank;
+  const double *const *init_factors;    /* host FP64 ColMajor I_k x R */
+  double *const *out_factors;           /* host FP64 ColMajor I_k x R */
+  double threshold_error;               /* this instance's stop target (<= 0: opts->threshold_error) */
+} ptg_cpd_instance;
+int ptg_cpd_batched(ptg_ctx *ctx, int n, const ptg_cpd_instance *instances, const ptg_cpd_options *opts,
+                    ptg_cpd_result *results, double *converge_seconds);
+
 /* ---- Learned warm start (no counterpart in the reference) ------------------------------
  * A two-hidden-layer ReLU network (128 units) maps the features of an NNLS row -- the
  * MTTKRP row divided by its norm and eight scale-free summaries of the Hadamard-of-Grams

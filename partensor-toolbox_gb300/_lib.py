@@ -22,7 +22,7 @@ EXPORTS = [
     "ptg_ctx_synchronize", "ptg_ctx_set_option", "ptg_ctx_enable_stats", "ptg_ctx_get_stats", "ptg_ctx_reset_stats",
     "ptg_tensor_create", "ptg_tensor_destroy", "ptg_tensor_norms",
     "ptg_mttkrp", "ptg_cpd_default_options", "ptg_cpd_als", "ptg_cpd",
-    "ptg_cpd_dimtree_als", "ptg_cpd_dimtree", "ptg_mttkrp_noalloc",
+    "ptg_cpd_dimtree_als", "ptg_cpd_dimtree", "ptg_mttkrp_noalloc", "ptg_cpd_batched",
     "ptg_gtc_default_options", "ptg_gtc", "ptg_gtc_sort_mode",
     "ptg_mlp_create", "ptg_mlp_destroy", "ptg_mlp_num_params", "ptg_mlp_get_params", "ptg_mlp_set_params",
     "ptg_mlp_forward", "ptg_mlp_loss_grad", "ptg_mlp_train",
@@ -45,6 +45,14 @@ class CpdResult(ctypes.Structure):
                 ("accel_coeff", ctypes.c_int), ("accel_fail", ctypes.c_int),
                 ("refine_sweeps_done", ctypes.c_int), ("nesterov_iters_total", ctypes.c_longlong),
                 ("seconds_total", ctypes.c_double)]
+
+
+class CpdInstance(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int), ("dims", ctypes.c_int64 * MAX_ORDER),
+                ("tensor", ctypes.POINTER(ctypes.c_double)), ("rank", ctypes.c_int),
+                ("init_factors", ctypes.POINTER(ctypes.POINTER(ctypes.c_double))),
+                ("out_factors", ctypes.POINTER(ctypes.POINTER(ctypes.c_double))),
+                ("threshold_error", ctypes.c_double)]
 
 
 class SweepTrace(ctypes.Structure):
@@ -130,6 +138,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ptg_mlp_train.argtypes = [vp, vp, vp, vp, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                   ctypes.c_ulonglong, dp]
     lib.ptg_cpd_dimtree_als.argtypes = lib.ptg_cpd_als.argtypes
+    lib.ptg_cpd_batched.argtypes = [vp, ctypes.c_int, ctypes.POINTER(CpdInstance), ctypes.POINTER(CpdOptions),
+                                    ctypes.POINTER(CpdResult), dp]
     lib.ptg_cpd_dimtree.argtypes = lib.ptg_cpd.argtypes
     for name in EXPORTS:
         if name not in ("ptg_last_error", "ptg_version", "ptg_cpd_default_options", "ptg_gtc_default_options",

@@ -16,7 +16,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import CpdOptions, CpdResult, SweepTrace, check
+from ._lib import CpdInstance, CpdOptions, CpdResult, SweepTrace, check
 
 UNCONSTRAINED, NONNEGATIVITY, ORTHOGONALITY, SPARSITY, CONSTANT = 0, 1, 2, 3, 4
 DTYPES = {"f32": _lib.PTG_F32, "fp32": _lib.PTG_F32, "bf16": _lib.PTG_BF16}
@@ -320,3 +320,48 @@ def cpdDimTree(tnsX, R: int, options: Optional[Options] = None,
     """partensor::cpdDimTree(execution::cuda, tnsX, R[, options][, factorsInit])
     (include/CpdDimTree.hpp:809-1362) with a host FP64 tensor (``ptg_cpd_dimtree``)."""
     return cpd(tnsX, R, options, factorsInit, dims=dims, ctx=ctx, _dimtree=True)
+
+
+def cpd_batched(problems: Sequence[tuple], options: Optional[Options] = None,
+                ctx: Optional[Context] = None) -> tuple[list[Status], np.ndarray]:
+    """Many independent nonnegative CPDs in one call (``ptg_cpd_batched``): ``problems`` is a
+    sequence of (tnsX, R, factorsInit) or (tnsX, R, factorsInit, threshold_error) with host
+    FP64 tensors of the same order (the optional 4th item is that instance's stop target,
+    otherwise ``options.threshold_error``).  Returns
+    the per-instance Status list (``seconds``: from the call's start until the instance's
+    stop test passed) and the same times counted from the start of the ALS loop, once every
+    tensor is resident.  The reference has no batched form; this is the
+    loop ``for p in problems: partensor::cpd(p...)`` (include/Cpd.hpp:534-577) in one call."""
+    ctx = ctx or default_context()
+    n = len(problems)
+    if n == 0:
+        return [], np.zeros(0)
+    keep = []
+    insts = (CpdInstance * n)()
+    outs_all = []
+    N = None
+    for i, prob in enumerate(problems):
+        X, R, init = prob[:3]
+        insts[i].threshold_error = float(prob[3]) if len(prob) > 3 else 0.0
+        a = np.asarray(X, dtype=np.float64)
+        N = a.ndim if N is None else N
+        flat = np.asfortranarray(a).reshape(-1, order="F")
+        inits = [np.asfortranarray(np.asarray(f, dtype=np.float64)) for f in init]
+        outs = [np.zeros((a.shape[k], R), order="F") for k in range(a.ndim)]
+        ip = (ctypes.POINTER(ctypes.c_double) * a.ndim)(*[_dptr(x) for x in inits])
+        op = (ctypes.POINTER(ctypes.c_double) * a.ndim)(*[_dptr(x) for x in outs])
+        keep += [flat, inits, ip, op]
+        outs_all.append(outs)
+        insts[i].order = a.ndim
+        for k in range(a.ndim):
+            insts[i].dims[k] = a.shape[k]
+        insts[i].tensor = _dptr(flat)
+        insts[i].rank = int(R)
+        insts[i].init_factors = ctypes.cast(ip, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)))
+        insts[i].out_factors = ctypes.cast(op, ctypes.POINTER(ctypes.POINTER(ctypes.c_double)))
+    options = options or Options(order=N)
+    res = (CpdResult * n)()
+    secs = np.zeros(n)
+    check(ctx._lib.ptg_cpd_batched(ctx.handle, n, insts, ctypes.byref(options.to_c()), res,
+                                   secs.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return [_status_from(options, outs_all[i], res[i], None, 0) for i in range(n)], secs

@@ -230,6 +230,7 @@ int ptg_ctx_destroy(ptg_ctx *c) {
   stats_resolve(c);
   for (cudaEvent_t e : c->stats.pool) cudaEventDestroy(e);
   if (c->dev_err) cudaFree(c->dev_err);
+  if (c->pinned) cudaFreeHost(c->pinned);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->side) cudaStreamDestroy(c->side);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -69,6 +70,9 @@ struct ptg_ctx {
   ptg_ctx_stats stats;
   int mttkrp_impl = 0;                // PTG_OPT_MTTKRP_IMPL
   int *dev_err = nullptr;             // device error word written by bounded waits
+  std::map<std::string, int> tuned;   // autotuner choices (batched CPD split-K target)
+  void *pinned = nullptr;             // page-locked host staging, kept between calls
+  size_t pinned_bytes = 0;
 };
 
 struct ptg_tensor {
@@ -134,6 +138,23 @@ int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &
 // Reads and clears the device error word (synchronises the stream first).
 int check_device_error(ptg_ctx *ctx);
 
+// A batch of MTTKRP-shaped contractions (one per instance, same layout class, FP32
+// storage) planned once into a device work list of (member, m-tile, K-split) items; all
+// members run in one launch, then one launch sums each member's split partials.  Pointers
+// are fixed at planning time, so a launch can be captured in a CUDA graph.
+struct BatchedContraction {
+  void *mem = nullptr;                 // one allocation: params, items, reduce descriptors, partials
+  void *params = nullptr, *items = nullptr, *reduce = nullptr;
+  int nitems = 0, nmembers = 0, BN = 0;
+  bool mmajor = false;
+  void release();
+};
+int batched_plan(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, const std::vector<Contraction> &cs,
+                 const std::vector<int> &ranks, const std::vector<float *> &outs, const std::vector<int> &insts,
+                 int bn, int target_per_sm, BatchedContraction *bc);
+// active[inst] == 0 skips that instance's items (nullptr: all run).
+int batched_launch(ptg_ctx *ctx, const BatchedContraction &bc, const int *active, cudaStream_t stream);
+
 // Statistics helpers: count kernel launches; bracket a contraction with events.
 inline void count_launches(ptg_ctx *ctx, int n) { ctx->stats.launches += n; }
 int stats_begin(ptg_ctx *ctx, cudaStream_t s, cudaEvent_t *ev);
@@ -181,5 +202,24 @@ int launch_accel_combine(const float *const *cur, const float *const *old, float
 // of grams[0..order-2].
 int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const float *const *grams,
                       int order, int R, double *out2, cudaStream_t stream);
+
+// Batched many-instance CPD (ptg_batched.cu, ptg_solve.cu).
+struct EigDesc {            // eigenbounds of one instance and mode
+  const float *gram[PTG_MAX_ORDER];
+  int order, mode, R, inst;
+  NnlsParams *out;
+};
+struct InstDesc {           // device buffers of one instance
+  float *fac[PTG_MAX_ORDER], *old[PTG_MAX_ORDER], *acc[PTG_MAX_ORDER];
+  float *gram[PTG_MAX_ORDER], *gacc[PTG_MAX_ORDER];
+  int rows[PTG_MAX_ORDER];
+  int order, R, weight, inst;
+  float *M;                 // last MTTKRP result of the instance [max rows][R]
+  double *cost_out;         // [2]
+};
+enum class BatchedOp { Gram, GramAcc, Normalize, AccelCombine, CopyOld, Select, CostTerms, CostTermsAcc };
+int launch_eigen_batched(ptg_ctx *ctx, const EigDesc *d, int n, const int *active, cudaStream_t s);
+int launch_batched_op(ptg_ctx *ctx, BatchedOp op, const InstDesc *d, int n, const int *flag, const float *step,
+                      cudaStream_t s);
 
 }  // namespace ptg

@@ -111,7 +111,7 @@ constexpr int BK = 32;
 // MMAJOR: mode-0 style (P == 1): q contiguous; tile [BK s][BM q]  -> Xs[k][m]
 // KMAJOR: P > 1: p contiguous within (q, s); tile [BM q][BK p]   -> Xs[m][k]
 template <typename T, int BN, bool MMAJOR>
-__global__ void __launch_bounds__(kThreads) mttkrp_simt_kernel(const SimtParams prm) {
+__device__ __forceinline__ void mttkrp_simt_body(const SimtParams &prm, int mtile, int split) {
   using C = Cfg<BN>;
   constexpr int BM = C::BM, TM = C::TM, TN = C::TN;
   constexpr int NG = BN / TN;  // column groups
@@ -128,8 +128,7 @@ __global__ void __launch_bounds__(kThreads) mttkrp_simt_kernel(const SimtParams 
 
   const int tid = threadIdx.x;
   const int ng = tid % NG, mg = tid / NG;
-  const int64_t q0 = (int64_t)blockIdx.x * BM;
-  const int split = blockIdx.y;
+  const int64_t q0 = (int64_t)mtile * BM;
   const int64_t t_begin = (int64_t)split * prm.ktiles_per_split;
   const int64_t t_end = min(prm.ktiles_total, t_begin + prm.ktiles_per_split);
   const T *X = reinterpret_cast<const T *>(prm.X);
@@ -307,6 +306,11 @@ __global__ void __launch_bounds__(kThreads) mttkrp_simt_kernel(const SimtParams 
             make_float4(acc[i][j], acc[i][j + 1], acc[i][j + 2], acc[i][j + 3]);
     }
   }
+}
+
+template <typename T, int BN, bool MMAJOR>
+__global__ void __launch_bounds__(kThreads) mttkrp_simt_kernel(const SimtParams prm) {
+  mttkrp_simt_body<T, BN, MMAJOR>(prm, blockIdx.x, blockIdx.y);
 }
 
 // out[q, col0 + c] = sum over splits of partial[split][q][c], in split order.
@@ -496,6 +500,172 @@ int simt_mttkrp_fixed_scratch(const ptg_tensor *t, const Contraction &c, int R, 
   if (R <= 64) return launch_cfg_fixed<64>(t, c, R, 0, out, stream, sm_count, scratch, cap_floats);
   for (int c0 = 0; c0 < R; c0 += 128)
     PTG_TRY(launch_cfg_fixed<128>(t, c, R, c0, out, stream, sm_count, scratch, cap_floats));
+  return PTG_OK;
+}
+
+namespace {
+
+template <int BN, bool MMAJOR>
+__global__ void __launch_bounds__(kThreads)
+mttkrp_simt_batched_kernel(const SimtParams *__restrict__ prms, const int4 *__restrict__ items,
+                           const int *__restrict__ active) {
+  const int4 it = items[blockIdx.x];   // (member, m-tile, split, instance)
+  if (active && !active[it.w]) return;
+  mttkrp_simt_body<float, BN, MMAJOR>(prms[it.x], it.y, it.z);
+}
+
+struct ReduceDesc {
+  const float *partial;
+  float *out;
+  int64_t Q, q_write;
+  int nsplit, BN, R, inst;
+};
+
+__global__ void batched_reduce_kernel(const ReduceDesc *__restrict__ d, const int *__restrict__ active) {
+  const ReduceDesc r = d[blockIdx.x];
+  if (active && !active[r.inst]) return;
+  const int64_t n = r.q_write * r.R;
+  for (int64_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
+    const int64_t q = idx / r.R;
+    const int c = (int)(idx % r.R);
+    float s = 0.0f;
+    for (int sp = 0; sp < r.nsplit; ++sp) s += r.partial[((int64_t)sp * r.Q + q) * r.BN + c];
+    r.out[q * r.R + c] = s;
+  }
+}
+
+template <int BN>
+int batched_plan_bn(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, const std::vector<Contraction> &cs,
+                    const std::vector<int> &ranks, const std::vector<float *> &outs, const std::vector<int> &insts,
+                    int target_per_sm, BatchedContraction *bc) {
+  using Cf = Cfg<BN>;
+  const size_t m = cs.size();
+  std::vector<SimtParams> prms(m);
+  std::vector<int4> items;
+  std::vector<ReduceDesc> red(m);
+  std::vector<size_t> part_off(m);
+  size_t part_total = 0;
+  // total work, to size every member's split count in proportion to its share
+  double work_total = 0.0;
+  for (size_t i = 0; i < m; ++i) work_total += (double)cs[i].P * cs[i].Q * cs[i].S;
+  const double target_ctas = (double)ctx->sm_count * target_per_sm;
+  bool mmajor = false;
+  for (size_t i = 0; i < m; ++i) {
+    const Contraction &c = cs[i];
+    mmajor = (c.P == 1);
+    SimtParams &prm = prms[i];
+    prm = SimtParams{};
+    prm.X = ts[i]->data;
+    prm.P = c.P;
+    prm.Q = c.Q;
+    prm.S = c.S;
+    prm.before = to_dev(c.before);
+    prm.after = to_dev(c.after);
+    prm.R = ranks[i];
+    prm.col0 = 0;
+    prm.out = outs[i];
+    prm.q_write = c.q_write;
+    prm.ldo = ranks[i];
+    if (mmajor) {
+      prm.pblocks = 1;
+      prm.ktiles_total = (c.S + BK - 1) / BK;
+    } else {
+      prm.pblocks = (c.P + BK - 1) / BK;
+      prm.ktiles_total = c.S * prm.pblocks;
+    }
+    const int64_t mtiles = (c.Q + Cf::BM - 1) / Cf::BM;
+    const double share = ((double)c.P * c.Q * c.S) / work_total * target_ctas;
+    int64_t nsplit = std::max<int64_t>(1, (int64_t)(share / (double)mtiles + 0.5));
+    nsplit = std::min<int64_t>(nsplit, prm.ktiles_total);
+    prm.ktiles_per_split = (prm.ktiles_total + nsplit - 1) / nsplit;
+    nsplit = (prm.ktiles_total + prm.ktiles_per_split - 1) / prm.ktiles_per_split;
+    prm.nsplit = (int)std::max<int64_t>(nsplit, 2);   // always through the partials
+    part_off[i] = part_total;
+    part_total += (size_t)nsplit * c.Q * BN;
+    for (int64_t mt = 0; mt < mtiles; ++mt)
+      for (int64_t sp = 0; sp < nsplit; ++sp) items.push_back(make_int4((int)i, (int)mt, (int)sp, insts[i]));
+    red[i] = ReduceDesc{nullptr, outs[i], c.Q, c.q_write, (int)nsplit, BN, ranks[i], insts[i]};
+  }
+  bc->release();
+  const size_t a1 = (sizeof(SimtParams) * m + 255) / 256 * 256;
+  const size_t a2 = (sizeof(int4) * items.size() + 255) / 256 * 256;
+  const size_t a3 = (sizeof(ReduceDesc) * m + 255) / 256 * 256;
+  cudaError_t e = cudaMalloc(&bc->mem, a1 + a2 + a3 + sizeof(float) * part_total + 256);
+  if (e != cudaSuccess) {
+    bc->mem = nullptr;
+    return cuda_error(e, "cudaMalloc(batched plan)", __FILE__, __LINE__);
+  }
+  char *b = (char *)bc->mem;
+  SimtParams *d_prm = (SimtParams *)b;
+  int4 *d_items = (int4 *)(b + a1);
+  ReduceDesc *d_red = (ReduceDesc *)(b + a1 + a2);
+  float *d_part = (float *)(b + a1 + a2 + a3);
+  for (size_t i = 0; i < m; ++i) {
+    prms[i].partial = d_part + part_off[i];
+    red[i].partial = d_part + part_off[i];
+  }
+  PTG_CUDA(cudaMemcpy(d_prm, prms.data(), sizeof(SimtParams) * m, cudaMemcpyHostToDevice));
+  PTG_CUDA(cudaMemcpy(d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
+  PTG_CUDA(cudaMemcpy(d_red, red.data(), sizeof(ReduceDesc) * m, cudaMemcpyHostToDevice));
+  bc->params = d_prm;
+  bc->items = d_items;
+  bc->reduce = d_red;
+  bc->nitems = (int)items.size();
+  bc->nmembers = (int)m;
+  bc->BN = BN;
+  bc->mmajor = mmajor;
+  return PTG_OK;
+}
+
+}  // namespace
+
+void BatchedContraction::release() {
+  if (mem) cudaFree(mem);
+  mem = params = items = reduce = nullptr;
+  nitems = nmembers = 0;
+}
+
+int batched_plan(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, const std::vector<Contraction> &cs,
+                 const std::vector<int> &ranks, const std::vector<float *> &outs, const std::vector<int> &insts,
+                 int bn, int target_per_sm, BatchedContraction *bc) {
+  if (cs.empty()) return PTG_OK;
+  for (const ptg_tensor *t : ts)
+    if (t->dtype != PTG_F32) return set_error(PTG_ERR_UNSUPPORTED, "batched MTTKRP: FP32 storage only");
+  const bool mm = cs[0].P == 1;
+  for (const Contraction &c : cs)
+    if ((c.P == 1) != mm) return set_error(PTG_ERR_INVALID, "internal: mixed layouts in one batch");
+  if (bn == 16) return batched_plan_bn<16>(ctx, ts, cs, ranks, outs, insts, target_per_sm, bc);
+  if (bn == 32) return batched_plan_bn<32>(ctx, ts, cs, ranks, outs, insts, target_per_sm, bc);
+  if (bn == 64) return batched_plan_bn<64>(ctx, ts, cs, ranks, outs, insts, target_per_sm, bc);
+  return set_error(PTG_ERR_UNSUPPORTED, "batched MTTKRP: rank > 64");
+}
+
+template <int BNV>
+static int batched_launch_bn(const BatchedContraction &bc, const int *active, cudaStream_t stream) {
+  const SimtParams *p = (const SimtParams *)bc.params;
+  const int4 *it = (const int4 *)bc.items;
+  const size_t smem = simt_smem_bytes<BNV>(bc.mmajor);
+  if (bc.mmajor) {
+    PTG_CUDA(cudaFuncSetAttribute(mttkrp_simt_batched_kernel<BNV, true>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    mttkrp_simt_batched_kernel<BNV, true><<<bc.nitems, kThreads, smem, stream>>>(p, it, active);
+  } else {
+    PTG_CUDA(cudaFuncSetAttribute(mttkrp_simt_batched_kernel<BNV, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    mttkrp_simt_batched_kernel<BNV, false><<<bc.nitems, kThreads, smem, stream>>>(p, it, active);
+  }
+  PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
+}
+
+int batched_launch(ptg_ctx *ctx, const BatchedContraction &bc, const int *active, cudaStream_t stream) {
+  if (!bc.nitems) return PTG_OK;
+  if (bc.BN == 16) PTG_TRY(batched_launch_bn<16>(bc, active, stream));
+  else if (bc.BN == 32) PTG_TRY(batched_launch_bn<32>(bc, active, stream));
+  else PTG_TRY(batched_launch_bn<64>(bc, active, stream));
+  batched_reduce_kernel<<<bc.nmembers, 256, 0, stream>>>((const ReduceDesc *)bc.reduce, active);
+  PTG_CUDA(cudaGetLastError());
+  count_launches(ctx, 2);
   return PTG_OK;
 }
 

@@ -81,8 +81,7 @@ __device__ int sturm_count_f64(const double *d, const double *e2, int n, double 
   return cnt;
 }
 
-__global__ void __launch_bounds__(kEigThreads)
-eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
+__device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R, NnlsParams *out) {
   __shared__ double A[kMaxR * kMaxR];
   __shared__ double v[kMaxR], p[kMaxR], w[kMaxR];
   __shared__ double d[kMaxR], e[kMaxR], e2[kMaxR];
@@ -277,6 +276,11 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
     out->status = (isfinite(L) && isfinite(mu)) ? 0 : PTG_ERR_NUMERIC;
     s_scalar[0] = L;
   }
+}
+
+__global__ void __launch_bounds__(kEigThreads)
+eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
+  eigen_bounds_body(gp, order, mode, R, out);
 }
 
 // ------------------------------------------------------------------------------------
@@ -929,6 +933,173 @@ int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const
   for (int k = 0; k < order; ++k) gp.g[k] = grams[k];
   cost_terms_kernel<<<1, 512, 0, stream>>>(M, A_last, I_last * R, gp, order, R, out2);
   PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
+}
+
+}  // namespace ptg
+
+// ------------------------------------------------------------------------------------
+// Batched forms for many small instances (one CTA per instance; inactive instances
+// return at once).  Each reuses the single-instance arithmetic above.
+// ------------------------------------------------------------------------------------
+namespace ptg {
+namespace {
+
+__global__ void __launch_bounds__(kEigThreads) eigen_batched_kernel(const EigDesc *__restrict__ d,
+                                                                    const int *__restrict__ active) {
+  const EigDesc &e = d[blockIdx.x];
+  if (active && !active[e.inst]) return;
+  GramPtrs gp{};
+  for (int k = 0; k < e.order; ++k) gp.g[k] = e.gram[k];
+  eigen_bounds_body(gp, e.order, e.mode, e.R, e.out);
+}
+
+// G_k = A_k^T A_k for every factor of the instance (fac or acc set).
+__global__ void gram_batched_kernel(const InstDesc *__restrict__ d, const int *__restrict__ active, int use_acc) {
+  const InstDesc &in = d[blockIdx.x];
+  if (active && !active[in.inst]) return;
+  const int R = in.R;
+  for (int k = 0; k < in.order; ++k) {
+    const float *A = use_acc ? in.acc[k] : in.fac[k];
+    float *G = use_acc ? in.gacc[k] : in.gram[k];
+    for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
+      const int a = idx / R, b = idx % R;
+      float s = 0.f;
+      for (int i = 0; i < in.rows[k]; ++i) s = fmaf(A[(size_t)i * R + a], A[(size_t)i * R + b], s);
+      G[idx] = s;
+    }
+  }
+}
+
+__global__ void normalize_batched_kernel(const InstDesc *__restrict__ d, const int *__restrict__ active) {
+  const InstDesc &in = d[blockIdx.x];
+  if (active && !active[in.inst]) return;
+  __shared__ float mult[PTG_MAX_ORDER][64], lfs[PTG_MAX_ORDER][64];
+  NormArgs a{};
+  for (int k = 0; k < in.order; ++k) {
+    a.fac[k] = in.fac[k];
+    a.gram[k] = in.gram[k];
+    a.rows[k] = in.rows[k];
+  }
+  a.order = in.order;
+  a.weight = in.weight;
+  a.R = in.R;
+  for (int c = threadIdx.x; c < a.R; c += blockDim.x) {
+    float m[PTG_MAX_ORDER], l[PTG_MAX_ORDER];
+    normalize_column(a, c, m, l);
+    for (int k = 0; k < a.order; ++k) {
+      mult[k][c] = m[k];
+      lfs[k][c] = l[k];
+    }
+  }
+  __syncthreads();   // every Gram diagonal is read before any Gram is written
+  for (int k = 0; k < a.order; ++k)
+    for (int idx = threadIdx.x; idx < a.rows[k] * a.R; idx += blockDim.x) a.fac[k][idx] *= mult[k][idx % a.R];
+  const int N = a.order, last = N - 1, w = a.weight, R = a.R;
+  for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
+    const int r1 = idx / R, r2 = idx % R;
+    float wm = 1.0f;
+    for (int j = 0; j < last; ++j) {
+      if (j == w) continue;
+      const float nm = lfs[j][r1] * lfs[j][r2];
+      wm *= nm;
+      a.gram[j][idx] = a.gram[j][idx] / nm;
+    }
+    a.gram[w][idx] *= wm;
+  }
+}
+
+// acc = old + step (fac - old) for instances with accel[inst] != 0 (step[inst]).
+__global__ void accel_combine_batched_kernel(const InstDesc *__restrict__ d, const int *__restrict__ accel,
+                                             const float *__restrict__ step) {
+  const InstDesc &in = d[blockIdx.x];
+  if (!accel[in.inst]) return;
+  const float s = step[in.inst];
+  for (int k = 0; k < in.order; ++k)
+    for (int idx = threadIdx.x; idx < in.rows[k] * in.R; idx += blockDim.x) {
+      const float o = in.old[k][idx];
+      in.acc[k][idx] = o + s * (in.fac[k][idx] - o);
+    }
+}
+
+// old = fac for instances with flag[inst] != 0
+__global__ void copy_old_batched_kernel(const InstDesc *__restrict__ d, const int *__restrict__ flag) {
+  const InstDesc &in = d[blockIdx.x];
+  if (!flag[in.inst]) return;
+  for (int k = 0; k < in.order; ++k)
+    for (int idx = threadIdx.x; idx < in.rows[k] * in.R; idx += blockDim.x) in.old[k][idx] = in.fac[k][idx];
+}
+
+// fac, gram = acc, gacc for instances with accepted[inst] != 0
+__global__ void select_batched_kernel(const InstDesc *__restrict__ d, const int *__restrict__ accepted) {
+  const InstDesc &in = d[blockIdx.x];
+  if (!accepted[in.inst]) return;
+  for (int k = 0; k < in.order; ++k) {
+    for (int idx = threadIdx.x; idx < in.rows[k] * in.R; idx += blockDim.x) in.fac[k][idx] = in.acc[k][idx];
+    for (int idx = threadIdx.x; idx < in.R * in.R; idx += blockDim.x) in.gram[k][idx] = in.gacc[k][idx];
+  }
+}
+
+// FP64 cost terms of a point: out[0] = <M, A_last>, out[1] = sum(Z_last .* G_last)
+__global__ void cost_terms_batched_kernel(const InstDesc *__restrict__ d, const int *__restrict__ flag,
+                                          int use_acc) {
+  const InstDesc &in = d[blockIdx.x];
+  if (flag && !flag[in.inst]) return;
+  const int last = in.order - 1, R = in.R;
+  const float *A = use_acc ? in.acc[last] : in.fac[last];
+  float *const *G = use_acc ? in.gacc : in.gram;
+  __shared__ double red[2][32];
+  double s = 0.0, h = 0.0;
+  for (int64_t idx = threadIdx.x; idx < (int64_t)in.rows[last] * R; idx += blockDim.x)
+    s = fma((double)in.M[idx], (double)A[idx], s);
+  for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
+    double z = 1.0;
+    for (int k = last - 1; k >= 0; --k) z *= (double)G[k][idx];
+    h = fma(z, (double)G[last][idx], h);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, o);
+    h += __shfl_down_sync(0xffffffffu, h, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = s;
+    red[1][threadIdx.x >> 5] = h;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += red[0][w];
+      b += red[1][w];
+    }
+    in.cost_out[0] = a;
+    in.cost_out[1] = b;
+  }
+}
+
+}  // namespace
+
+int launch_eigen_batched(ptg_ctx *ctx, const EigDesc *d, int n, const int *active, cudaStream_t s) {
+  eigen_batched_kernel<<<n, kEigThreads, 0, s>>>(d, active);
+  PTG_CUDA(cudaGetLastError());
+  count_launches(ctx, 1);
+  return PTG_OK;
+}
+
+int launch_batched_op(ptg_ctx *ctx, BatchedOp op, const InstDesc *d, int n, const int *flag, const float *step,
+                      cudaStream_t s) {
+  switch (op) {
+    case BatchedOp::Gram: gram_batched_kernel<<<n, 256, 0, s>>>(d, flag, 0); break;
+    case BatchedOp::GramAcc: gram_batched_kernel<<<n, 256, 0, s>>>(d, flag, 1); break;
+    case BatchedOp::Normalize: normalize_batched_kernel<<<n, 256, 0, s>>>(d, flag); break;
+    case BatchedOp::AccelCombine: accel_combine_batched_kernel<<<n, 256, 0, s>>>(d, flag, step); break;
+    case BatchedOp::CopyOld: copy_old_batched_kernel<<<n, 256, 0, s>>>(d, flag); break;
+    case BatchedOp::Select: select_batched_kernel<<<n, 256, 0, s>>>(d, flag); break;
+    case BatchedOp::CostTerms: cost_terms_batched_kernel<<<n, 256, 0, s>>>(d, flag, 0); break;
+    case BatchedOp::CostTermsAcc: cost_terms_batched_kernel<<<n, 256, 0, s>>>(d, flag, 1); break;
+  }
+  PTG_CUDA(cudaGetLastError());
+  count_launches(ctx, 1);
   return PTG_OK;
 }
 

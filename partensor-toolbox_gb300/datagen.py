@@ -95,3 +95,51 @@ def factors_colmajor(A: torch.Tensor) -> torch.Tensor:
 
 def from_colmajor(buf: torch.Tensor, rows: int, cols: int) -> torch.Tensor:
     return buf.reshape(cols, rows).t()
+
+
+@dataclasses.dataclass
+class BatchInstance:
+    X: "np.ndarray"                 # float64 [I0, I1, I2]
+    rank: int
+    init_factors: list
+    true_factors: list
+    noise_rel: float
+
+
+def make_fmri_batch(n: int = 256, seed: int = 4, snr_db: float = 15.0,
+                    voxels=(32, 128), time=(100, 400), trials=(16, 64), ranks=(8, 12, 16, 24),
+                    init_seed: int | None = None) -> list:
+    """Uneven fMRI-like CPD instances (voxels x time x subjects-trials): per instance the
+    dims are drawn uniformly from the three ranges and the rank from ``ranks``; spatial
+    maps are nonnegative and sparse (Bernoulli(0.2) x U[0,1]), temporal factors are white
+    noise filtered by a Gaussian kernel of width 5 (shifted to be nonnegative), trial
+    loadings are U[0,1]; Gaussian noise at ``snr_db``.  Initial factors U[0,1] from
+    ``init_seed`` (default seed + 1).  Seeded numpy generators; host FP64 tensors."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    rng_init = np.random.default_rng(seed + 1 if init_seed is None else init_seed)
+    t = np.arange(-15, 16)
+    kern = np.exp(-0.5 * (t / 5.0) ** 2)
+    kern /= kern.sum()
+    out = []
+    for _ in range(n):
+        I0 = int(rng.integers(voxels[0], voxels[1] + 1))
+        I1 = int(rng.integers(time[0], time[1] + 1))
+        I2 = int(rng.integers(trials[0], trials[1] + 1))
+        R = int(ranks[int(rng.integers(0, len(ranks)))])
+        S = (rng.random((I0, R)) < 0.2) * rng.random((I0, R))
+        # a column that drew no voxel gets one, so every component is present
+        for r in np.nonzero(S.sum(0) == 0)[0]:
+            S[int(rng.integers(0, I0)), r] = rng.random()
+        W = rng.standard_normal((I1 + len(t) - 1, R))
+        Tm = np.stack([np.convolve(W[:, r], kern, mode="valid") for r in range(R)], axis=1)
+        Tm = Tm - Tm.min(0, keepdims=True)
+        C = rng.random((I2, R))
+        X = np.einsum("ir,jr,kr->ijk", S, Tm, C)
+        sigma = np.sqrt((X ** 2).sum() / (X.size * 10 ** (snr_db / 10)))
+        noise = sigma * rng.standard_normal(X.shape)
+        Xn = np.asfortranarray(X + noise)   # ColMajor, the layout the C ABI reads without a copy
+        noise_rel = float(np.linalg.norm(noise) / np.linalg.norm(Xn))
+        init = [rng_init.random((I, R)) for I in (I0, I1, I2)]
+        out.append(BatchInstance(Xn, R, init, [S, Tm, C], noise_rel))
+    return out

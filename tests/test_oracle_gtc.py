@@ -1,0 +1,100 @@
+"""CPU tests of the GTC oracle (oracle/gtc.py) and of the warm-start MLP oracle."""
+import functools
+
+import numpy as np
+import pytest
+
+from oracle import cpd as oc
+from oracle import gtc as og
+from oracle import mlp as om
+
+
+def sort_rows_literal(N, mode):
+    """SortRows<N, mode> (include/TensorOperations.hpp:622-666) restated line by line as a
+    comparator: sort_direction = {mode, last (or last-1), then downwards skipping mode}."""
+    direction = [mode, N - 1 if mode < N - 1 else N - 2]
+    for i in range(2, N):
+        d = direction[i - 1] - 1
+        if d == mode:
+            d -= 1
+        direction.append(d)
+
+    def less(v1, v2):
+        prev_equal = False
+        for i in range(N):
+            a, b = v1[direction[i]], v2[direction[i]]
+            if i == 0:
+                if a < b:
+                    return True
+                prev_equal = a == b
+            else:
+                if prev_equal and a < b:
+                    return True
+                prev_equal = prev_equal and a == b
+        return False
+
+    return lambda x, y: -1 if less(x, y) else (1 if less(y, x) else 0)
+
+
+@pytest.mark.parametrize("dims", [(7, 5, 4), (4, 3, 5, 2)])
+def test_sort_key_equals_sortrows(dims):
+    idx, vals, _ = og.make_gtc_problem(dims, 60, 2, seed=1)
+    N = len(dims)
+    rows = [list(idx[:, e]) + [e] for e in range(idx.shape[1])]
+    for mode in range(N):
+        ref = sorted(rows, key=functools.cmp_to_key(sort_rows_literal(N, mode)))
+        got = og.matricize(idx, vals, dims, mode).perm
+        assert [r[-1] for r in ref] == list(got)
+
+
+def test_sparse_mttkrp_matches_dense():
+    dims, R = (9, 8, 7), 3
+    idx, vals, _ = og.make_gtc_problem(dims, 150, R, seed=2)
+    rng = np.random.default_rng(3)
+    f = [rng.random((I, R)) for I in dims]
+    Xd = np.zeros(dims)
+    Xd[tuple(idx)] = vals
+    for n in range(3):
+        assert np.allclose(og.sparse_mttkrp(f, og.matricize(idx, vals, dims, n)), oc.mttkrp(f, Xd, n))
+
+
+def test_power_method_reaches_top_eigenvalue():
+    rng = np.random.default_rng(4)
+    K = rng.random((50, 6))
+    H = K.T @ K
+    assert og.power_method(H, 1e-9) == pytest.approx(np.linalg.eigvalsh(H).max(), rel=1e-8)
+
+
+def test_gtc_decreases_cost_and_stochastic_is_deterministic():
+    dims, R = (20, 18, 16), 3
+    idx, vals, _ = og.make_gtc_problem(dims, 1500, R, seed=5)
+    rng = np.random.default_rng(6)
+    init = [rng.random((I, R)) for I in dims]
+    st = og.gtc(idx, vals, dims, R, og.SparseOptions(order=3, max_iter=4, lambdas=[1e-3] * 3), init)
+    rels = [t["rel"] for t in st.trace]
+    assert rels[-1] < rels[0]
+    o = og.SparseOptions(order=3, max_iter=1, c_stochastic_perc=0.2, lambdas=[1e-3] * 3, seed=9)
+    a = og.gtc_stochastic(idx, vals, dims, R, o, init)
+    b = og.gtc_stochastic(idx, vals, dims, R, o, init)
+    for k in range(3):
+        assert np.array_equal(a.factors[k], b.factors[k])
+
+
+def test_pivot_hash_known_values():
+    # splitmix64 finaliser of the mixed coordinates (the GPU sampler uses the same arithmetic)
+    assert og.pivot_hash(0, 0, 0, 0, 0) == 0
+    assert og.pivot_hash(1, 2, 3, 4, 5) == og.pivot_hash(1, 2, 3, 4, 5)
+    assert og.pivot_hash(1, 2, 3, 4, 5) != og.pivot_hash(1, 2, 3, 4, 6)
+
+
+def test_mlp_gradient_finite_differences():
+    din, h, dout = 5, 8, 3
+    rng = np.random.default_rng(7)
+    theta = om.init(din, h, dout, 2) + 0.01 * rng.standard_normal(om.nparams(din, h, dout))
+    X, T = rng.standard_normal((6, din)), rng.standard_normal((6, dout))
+    _, g = om.loss_and_grad(theta, X, T, din, h, dout)
+    for i in range(len(theta)):
+        e = np.zeros_like(theta)
+        e[i] = 1e-6
+        fd = (om.loss_and_grad(theta + e, X, T, din, h, dout)[0] - om.loss_and_grad(theta - e, X, T, din, h, dout)[0]) / 2e-6
+        assert fd == pytest.approx(g[i], rel=1e-4, abs=1e-9)
