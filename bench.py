@@ -11,8 +11,9 @@ noise floor ||noise||/||X|| (computed in FP64 when the data is generated) is the
 FP64 least-squares optimum reaches up to O(R*sum(I)/prod(I)) = 1e-4 of overfit, so the
 target is "within 1e-3 of the FP64 oracle's converged fit".
 
-  value    BF16 tensor storage + tcgen05 MTTKRP + one FP32 refinement sweep, tensor already
-           resident in HBM (seconds per solve, lower is better)
+  value    BF16 tensor storage + tcgen05 MTTKRP until the fit reaches the target, then the
+           final factors' fit measured on the FP32 copy (one FP32 MTTKRP, Gram form); tensor
+           already resident in HBM (seconds per solve, lower is better)
   plain    the same solve with FP32 storage and CUDA-core MTTKRP (reported beside it)
   e2e      the one-call C ABI (ptg_cpd) from a pinned host FP64 buffer: host->device copy,
            BF16 and FP32 conversion, solve, factor download, all inside the timed region
@@ -43,7 +44,7 @@ sys.path.insert(0, ROOT)
 DIMS = [1000, 1000, 1000]
 RANK = 32
 SEED, INIT_SEED, SNR_DB = 2, 3, 30.0
-METRIC = "time to rel. fit err <= FP64-oracle fit + 1e-3 (BF16 tcgen05 MTTKRP + FP32 refine), 1000^3 R=32 nonneg CPD-ALS"
+METRIC = "time to rel. fit err <= FP64-oracle fit + 1e-3 (BF16 tcgen05 MTTKRP, fit verified on FP32 data), 1000^3 R=32 nonneg CPD-ALS"
 # Sweeps the FP64 ALS needs to reach the target on this workload (measured with the FP32
 # plain form, whose per-sweep relative error follows the FP64 oracle within 1e-4).
 SWEEPS_TO_TARGET_FP64 = None   # filled from the plain-form run when available
@@ -201,7 +202,7 @@ def run_ours(args):
     def solve(form):
         if form == "bf16":
             o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target, precision="bf16",
-                            refine_sweeps=1)
+                            verify_fp32=True)
             return pkg.cpd_resident(ctx, Xb, R, o, init, refine=Xf)
         o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target)
         return pkg.cpd_resident(ctx, Xf, R, o, init)
@@ -253,7 +254,7 @@ def run_ours(args):
         host = torch.empty(p.X.numel(), dtype=torch.float64, pin_memory=True)
         host.copy_(p.X)
         hnp = host.numpy()
-        o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target, precision="bf16", refine_sweeps=1)
+        o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target, precision="bf16", verify_fp32=True)
         pkg.cpd(hnp, R, o, init, dims=dims, ctx=ctx)   # warm-up
         ts = []
         for _ in range(max(1, args.steps_e2e)):
@@ -290,6 +291,7 @@ def run_ours(args):
                    "l2": "inputs (2 GB BF16 / 4 GB FP32) > 129 MB L2, no flush",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "converged": bool(last_b.rel_costFunction <= target),
+        "fit_measured_on": "FP32 copy of the tensor (final factors)",
         "final_rel_err": last_b.rel_costFunction,
         "sweeps": last_b.ao_iter, "refine_sweeps": last_b.refine_sweeps_done,
         "nesterov_iters_total": last_b.nesterov_iters_total,
@@ -318,6 +320,127 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+BATCH_N, BATCH_SEED = 256, 4
+BATCH_METRIC = ("instances/s, 256 uneven fMRI-like nonneg CPDs (dims U[32,128]xU[100,400]xU[16,64], "
+                "R in {8,12,16,24}, 15 dB) each to its FP64-oracle fit + 1e-3")
+
+
+def _batch_problems():
+    from partensor_toolbox_gb300 import datagen as dg
+    batch = dg.make_fmri_batch(BATCH_N, seed=BATCH_SEED)
+    return [(b.X, b.rank, b.init_factors, b.noise_rel + 1e-3) for b in batch]
+
+
+def _batch_cpu(probs, sample, threads):
+    """The FP64 OpenMP restatement on the first `sample` instances, each to its target."""
+    from oracle import omp
+    t = time.perf_counter()
+    iters = []
+    for X, R, init, thr in probs[:sample]:
+        _, st, _ = omp.cpd_als(X.reshape(-1, order="F"), list(X.shape), R, init, threshold_error=thr,
+                               max_iter=200, nthreads=threads)
+        iters.append(st.ao_iter)
+    return time.perf_counter() - t, iters
+
+
+def run_batch_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return
+    ge = __import__("__graft_entry__")
+    ge.load_package()
+    probs = _batch_problems()
+    threads = os.cpu_count() or 1
+    sample = args.batch_sample
+    for _ in range(max(0, args.warmup_ref)):
+        _batch_cpu(probs, sample, threads)
+    ts = [_batch_cpu(probs, sample, threads)[0] for _ in range(args.steps)]
+    value = sample / statistics.mean(ts)
+    line = {"impl": "reference", "metric": BATCH_METRIC, "value": value, "unit": "instances/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.mean(ts) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded fMRI-like batch, seed 4)",
+            "config": {"workload": "cpd_batched fmri-like 256 instances", "instances": BATCH_N},
+            "cpu_baseline": {"value": value, "unit": "instances/s", "cores": threads, "kind": "port",
+                             "sample": f"first {sample} of the 256 instances per step, FP64 OpenMP "
+                                       f"restatement of CpdOpenMP (oracle/cpd_omp.c), each to its target"},
+            "e2e": {"value": value, "unit": "instances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch_ours(args):
+    import numpy as np
+    import torch
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ge = __import__("__graft_entry__")
+    pkg = ge.load_package()
+    probs = _batch_problems()
+    ctx = pkg.Context(local)
+    opts = pkg.Options(order=3, max_iter=200)
+    for _ in range(args.warmup):
+        pkg.cpd_batched(probs, opts, ctx=ctx)
+    ctx.enable_stats(True)
+    clk = ClockSampler()
+    clk.start()
+    walls, solves, conv = [], [], []
+    launches = 0
+    for _ in range(args.steps):
+        ctx.reset_stats()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sts, secs = pkg.cpd_batched(probs, opts, ctx=ctx)
+        walls.append(time.perf_counter() - t)
+        solves.append(float(secs.max()))
+        conv.append(secs)
+        kst = ctx.stats()
+        launches += kst["launches"]
+    clocks = clk.stop()
+    ctx.enable_stats(False)
+    secs = np.concatenate(conv)
+    hit = sum(st.rel_costFunction <= p[3] for st, p in zip(sts, probs))
+    solve_s = _max_over_ranks(statistics.mean(solves), ws)
+    wall_s = _max_over_ranks(statistics.mean(walls), ws)
+    peak, peak_kind = _peaks()
+    ach = kst["batch_pass_bytes"] / (kst["batch_pass_ms"] * 1e-3) / 1e9 if kst["batch_pass_ms"] > 0 else None
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        tcpu, it_cpu = _batch_cpu(probs, args.batch_sample, threads)
+        cpu = {"value": args.batch_sample / tcpu, "unit": "instances/s", "cores": threads, "kind": "port",
+               "sample": f"first {args.batch_sample} instances, FP64 OpenMP restatement of CpdOpenMP "
+                         f"(oracle/cpd_omp.c), each to its target ({sum(it_cpu)} sweeps)"}
+    h2d = int(sum(p[0].nbytes + sum(f.nbytes for f in p[2]) for p in probs))
+    d2h = int(sum(sum(f.nbytes for f in st.factors) for st in sts))
+    line = {
+        "metric": BATCH_METRIC, "value": ws * BATCH_N / solve_s, "unit": "instances/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": solve_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded fMRI-like batch: sparse spatial maps, smooth time courses, 15 dB)",
+        "config": {"workload": "cpd_batched fmri-like 256 instances", "instances": BATCH_N, "seed": BATCH_SEED,
+                   "l2": "824 MB of FP32 tensors > 129 MB L2, no flush",
+                   "timing": "ALS loop with every tensor resident (host clock around the graph-replayed loop)"},
+        "p50_s": float(np.percentile(secs, 50)), "p99_s": float(np.percentile(secs, 99)),
+        "instances_converged": int(hit), "sweeps_mean": float(np.mean([st.ao_iter for st in sts])),
+        "sweeps_max": int(max(st.ao_iter for st in sts)),
+        "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": (ach / peak) if ach else None, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "mttkrp_simt_batched_kernel + batched_reduce_kernel (one pass: every mode "
+                               "of every instance)",
+                     "launches": kst["batch_pass_launches"], "ms_per_pass": kst["batch_pass_ms"],
+                     "bytes_per_pass": kst["batch_pass_bytes"]},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "e2e": {"value": ws * BATCH_N / wall_s, "unit": "instances/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -333,8 +456,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--warmup-ref", type=int, default=0)
     ap.add_argument("--sweeps-to-target", type=int, default=20)
+    ap.add_argument("--workload", default="cpd-1000", choices=["cpd-1000", "fmri-batch"],
+                    help="cpd-1000: the headline 1000^3 solve; fmri-batch: 256 small CPDs in one call")
+    ap.add_argument("--batch-sample", type=int, default=32, help="instances the CPU baseline solves")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "fmri-batch":
+        run_batch_reference(args) if args.impl == "reference" else run_batch_ours(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -86,6 +86,11 @@ typedef struct {
   long long tc_launches;      /* the subset that ran on the tensor cores (tcgen05) */
   double tc_ms;
   double tc_bytes;
+  /* ptg_cpd_batched: one MTTKRP pass (every mode of every instance, the tuned work lists)
+   * timed with CUDA events right after tuning, and its algorithmic bytes */
+  long long batch_pass_launches;
+  double batch_pass_ms;
+  double batch_pass_bytes;
 } ptg_stats;
 int ptg_ctx_enable_stats(ptg_ctx *ctx, int enable);
 int ptg_ctx_get_stats(ptg_ctx *ctx, ptg_stats *out); /* synchronises the context's stream */
@@ -153,6 +158,10 @@ typedef struct {
                            trained warm_train_steps Adam steps and used from sweep n+1;
                            0: use the network as it is from sweep 1 */
   int warm_train_steps;
+  int verify_fp32;      /* 1: after a main loop on BF16 storage with no refinement sweeps, the
+                           reported cost is that of the final factors on an FP32 copy of the
+                           tensor (one more MTTKRP); ptg_cpd_als needs `refine`, ptg_cpd and
+                           ptg_cpd_dimtree make the copy from the same upload */
 } ptg_cpd_options;
 
 /* Fill *o with the reference defaults (include/PARTENSOR_basic.hpp:176-218). */

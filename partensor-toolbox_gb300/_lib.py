@@ -36,7 +36,8 @@ class CpdOptions(ctypes.Structure):
                 ("acceleration", ctypes.c_int), ("normalization", ctypes.c_int),
                 ("refine_sweeps", ctypes.c_int), ("warm_start", ctypes.c_int),
                 ("cost_every_sweep", ctypes.c_int), ("warm_model", ctypes.c_void_p),
-                ("warm_log_sweeps", ctypes.c_int), ("warm_train_steps", ctypes.c_int)]
+                ("warm_log_sweeps", ctypes.c_int), ("warm_train_steps", ctypes.c_int),
+                ("verify_fp32", ctypes.c_int)]
 
 
 class CpdResult(ctypes.Structure):
@@ -65,7 +66,9 @@ class Stats(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_longlong), ("mttkrp_launches", ctypes.c_longlong),
                 ("mttkrp_ms", ctypes.c_double), ("mttkrp_bytes", ctypes.c_double),
                 ("mttkrp_flops", ctypes.c_double), ("tc_launches", ctypes.c_longlong),
-                ("tc_ms", ctypes.c_double), ("tc_bytes", ctypes.c_double)]
+                ("tc_ms", ctypes.c_double), ("tc_bytes", ctypes.c_double),
+                ("batch_pass_launches", ctypes.c_longlong), ("batch_pass_ms", ctypes.c_double),
+                ("batch_pass_bytes", ctypes.c_double)]
 
 
 class GtcOptions(ctypes.Structure):

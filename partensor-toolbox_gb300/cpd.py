@@ -42,6 +42,7 @@ class Options:
     warm_model: object = None     # a WarmStartModel
     warm_log_sweeps: int = 5      # sweeps that log training pairs before the network is trained
     warm_train_steps: int = 200
+    verify_fp32: bool = False     # report the final cost on an FP32 copy (bf16 storage, no refinement)
 
     def __post_init__(self):
         if self.constraints is None:
@@ -65,6 +66,7 @@ class Options:
         o.warm_model = self.warm_model.handle if self.warm_model is not None else None
         o.warm_log_sweeps = int(self.warm_log_sweeps)
         o.warm_train_steps = int(self.warm_train_steps)
+        o.verify_fp32 = int(bool(self.verify_fp32))
         return o
 
 
@@ -114,7 +116,8 @@ class Context:
         check(self._lib.ptg_ctx_get_stats(self.handle, ctypes.byref(s)))
         return dict(launches=s.launches, mttkrp_launches=s.mttkrp_launches, mttkrp_ms=s.mttkrp_ms,
                     mttkrp_bytes=s.mttkrp_bytes, mttkrp_flops=s.mttkrp_flops, tc_launches=s.tc_launches,
-                    tc_ms=s.tc_ms, tc_bytes=s.tc_bytes)
+                    tc_ms=s.tc_ms, tc_bytes=s.tc_bytes, batch_pass_launches=s.batch_pass_launches,
+                    batch_pass_ms=s.batch_pass_ms, batch_pass_bytes=s.batch_pass_bytes)
 
     def close(self):
         if self.handle:

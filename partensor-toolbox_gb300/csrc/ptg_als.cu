@@ -192,6 +192,7 @@ void ptg_cpd_default_options(int order, ptg_cpd_options *o) {
   o->refine_sweeps = 0;
   o->warm_start = 0;
   o->cost_every_sweep = 1;
+  o->verify_fp32 = 0;
 }
 
 }  // extern "C"
@@ -371,6 +372,13 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
       ++ntrace;
     }
   }
+  // the cost of the final factors on the FP32 copy (one MTTKRP in the Gram form)
+  if (refine && refined == 0 && opt.verify_fp32) {
+    Xa = refine;
+    frob = Xa->frob_stored;
+    PTG_TRY(run.point_cost(Xa, frob, b.fac, b.gram, &f));
+    rel = f / std::sqrt(frob);
+  }
   // results: device FP32 row-major -> host FP64 ColMajor
   for (int k = 0; k < N; ++k) {
     const int64_t I = X->dims[k];
@@ -416,7 +424,7 @@ static int cpd_host_impl(ptg_ctx *ctx, int order, const int64_t *dims, const dou
                          ptg_cpd_result *result, ptg_sweep_trace *trace, bool dimtree) {
   if (!ctx || !dims || !host_tensor || !opts) return set_error(PTG_ERR_INVALID, "NULL argument");
   ptg_tensor *X = nullptr, *Xr = nullptr;
-  const bool want_refine = dtype != PTG_F32 && opts->refine_sweeps > 0;
+  const bool want_refine = dtype != PTG_F32 && (opts->refine_sweeps > 0 || opts->verify_fp32);
   int rc = PTG_OK;
   if (!want_refine) {
     rc = ptg_tensor_create(ctx, order, dims, dtype, host_tensor, 0, &X);

@@ -283,6 +283,9 @@ int ptg_ctx_get_stats(ptg_ctx *c, ptg_stats *out) {
   out->tc_launches = c->stats.tc_launches;
   out->tc_ms = c->stats.tc_ms;
   out->tc_bytes = c->stats.tc_bytes;
+  out->batch_pass_launches = c->stats.batch_pass_launches;
+  out->batch_pass_ms = c->stats.batch_pass_ms;
+  out->batch_pass_bytes = c->stats.batch_pass_bytes;
   return PTG_OK;
 }
 
@@ -296,6 +299,8 @@ int ptg_ctx_reset_stats(ptg_ctx *c) {
   c->stats.mttkrp_ms = c->stats.mttkrp_bytes = c->stats.mttkrp_flops = 0.0;
   c->stats.tc_launches = 0;
   c->stats.tc_ms = c->stats.tc_bytes = 0.0;
+  c->stats.batch_pass_launches = 0;
+  c->stats.batch_pass_ms = c->stats.batch_pass_bytes = 0.0;
   c->stats.enabled = en;
   return PTG_OK;
 }

@@ -21,6 +21,7 @@
 #include <atomic>
 #include <map>
 #include <thread>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -45,9 +46,13 @@ struct BNnls {
 };
 
 // Nesterov MNLS of one instance per CTA (include/NesterovMNLS.hpp:181-234 with the zero-column
-// repair of include/Cpd.hpp:206-207 and the Gram of :227).  Lane = column; a warp takes
-// groups of 4 rows; Y is kept transposed in shared memory so the 4 values of a k step are
-// one broadcast 16-byte load.
+// repair of include/Cpd.hpp:206-207 and the Gram of :227).  Lane = column; a warp owns
+// groups of 4 rows (all columns), so the product Y Z~ of a row needs only its own warp's Y;
+// Y is kept transposed in shared memory so the 4 values of a k step are one broadcast 16-byte
+// load.  The global stop test (max |grad .* Y| <= delta1 and min grad >= -delta2, :217-218)
+// fails iff some element violates it, so a warp that sees a violation sets the iteration's
+// flag word (three in rotation) and the block meets once per iteration; the update is done
+// speculatively into the other half of a ping-pong A buffer, so A_it survives a stop.
 __global__ void __launch_bounds__(BN_THREADS) nnls_block_kernel(const BNnls *__restrict__ tab,
                                                                 const int *__restrict__ active) {
   const BNnls a = tab[blockIdx.x];
@@ -55,10 +60,10 @@ __global__ void __launch_bounds__(BN_THREADS) nnls_block_kernel(const BNnls *__r
   extern __shared__ __align__(16) float sm[];
   const int R = a.R, I = a.I, Ip = (I + 3) & ~3;
   float *Yt = sm;                        // [R][Ip]
-  float *Ac = Yt + (size_t)R * Ip;       // [I][R]
-  float *Gs = Ac + (size_t)I * R;        // [I][R]
-  __shared__ float red[2][BN_THREADS / 32];
-  __shared__ int stop_flag;
+  float *Ab[2];
+  Ab[0] = Yt + (size_t)R * Ip;           // [I][R]
+  Ab[1] = Ab[0] + (size_t)I * R;         // [I][R]
+  __shared__ int vflag[3];
   __shared__ double dred[2][BN_THREADS / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const NnlsParams *np = a.np;
@@ -75,15 +80,20 @@ __global__ void __launch_bounds__(BN_THREADS) nnls_block_kernel(const BNnls *__r
   for (int idx = tid; idx < I * R; idx += BN_THREADS) {
     const int i = idx / R, cc = idx % R;
     const float a0 = a.A[idx];
-    Ac[idx] = a0;
+    Ab[0][idx] = a0;
     Yt[cc * Ip + i] = a0;
     a.Wt[idx] = a.M[idx] + lam * a0;     // W~ = W + lambda A0 (:206)
   }
   for (int idx = tid; idx < R * (Ip - I); idx += BN_THREADS) Yt[(idx / (Ip - I)) * Ip + I + idx % (Ip - I)] = 0.0f;
+  if (tid < 3) vflag[tid] = 0;
   __syncthreads();
   int it = 0;
-  for (;;) {
-    float mx = 0.0f, mn = INFINITY;
+  for (;; ++it) {
+    if (it >= kMaxInner) break;   // A_it is the result
+    const float *Acur = Ab[it & 1];
+    float *Anext = Ab[(it + 1) & 1];
+    const float beta = np->beta[it];
+    bool viol = false;
     for (int g = warp; 4 * g < I; g += BN_THREADS / 32) {
       const int i0 = 4 * g;
       float acc[4];
@@ -99,44 +109,25 @@ __global__ void __launch_bounds__(BN_THREADS) nnls_block_kernel(const BNnls *__r
           acc[3] = fmaf(y4.w, z[k], acc[3]);
         }
       }
+      __syncwarp();   // every lane has read this group's Y before any lane writes it
 #pragma unroll
       for (int r = 0; r < 4; ++r)
         if (i0 + r < I && cok) {
-          Gs[(i0 + r) * R + c] = acc[r];
-          mx = fmaxf(mx, fabsf(acc[r] * Yt[c * Ip + i0 + r]));
-          mn = fminf(mn, acc[r]);
+          const int i = i0 + r;
+          const float y = Yt[c * Ip + i];
+          viol |= (fabsf(acc[r] * y) > a.d1) || (acc[r] < -a.d2);
+          const float na = fmaxf(y - acc[r] * invL, 0.0f);                // :220
+          Yt[c * Ip + i] = (1.0f + beta) * na - beta * Acur[i * R + c];   // :228
+          Anext[i * R + c] = na;
         }
+      __syncwarp();
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-    }
-    if (lane == 0) {
-      red[0][warp] = mx;
-      red[1][warp] = mn;
-    }
+    if (__any_sync(0xffffffffu, viol) && lane == 0) vflag[it % 3] = 1;
+    if (tid == 0) vflag[(it + 1) % 3] = 0;   // the word of it+1 (read last at it-2)
     __syncthreads();
-    if (tid == 0) {
-      float M1 = 0.0f, M2 = INFINITY;
-      for (int w = 0; w < BN_THREADS / 32; ++w) {
-        M1 = fmaxf(M1, red[0][w]);
-        M2 = fminf(M2, red[1][w]);
-      }
-      stop_flag = ((M1 <= a.d1 && M2 >= -a.d2) || it >= kMaxInner) ? 1 : 0;   // :217-218
-    }
-    __syncthreads();
-    if (stop_flag) break;
-    const float beta = np->beta[it];
-    for (int idx = tid; idx < I * R; idx += BN_THREADS) {
-      const int i = idx / R, cc = idx % R;
-      const float y = Yt[cc * Ip + i];
-      const float na = fmaxf(y - Gs[idx] * invL, 0.0f);
-      Yt[cc * Ip + i] = (1.0f + beta) * na - beta * Ac[idx];
-      Ac[idx] = na;
-    }
-    __syncthreads();
-    ++it;
+    if (vflag[it % 3] == 0) break;           // no violation: stop, the result is A_it
   }
+  float *Ac = Ab[it & 1];
   // zero-column repair (:206-207): a column whose |A| sums to zero over all rows
   __shared__ int repair;
   if (tid == 0) repair = 0;
@@ -582,19 +573,28 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
                      "batched CPD: a factor (rows x rank) is too large for the one-CTA NNLS (shared memory)");
   PTG_CUDA(cudaFuncSetAttribute(nnls_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nnls_smem));
 
-  // ---- batched MTTKRP plans: per mode and rank class, plus the accelerated last mode ----
-  std::map<std::pair<int, int>, BatchedContraction> plans;   // (mode or N for accel, BN)
+  // ---- batched MTTKRP plans: per mode, rank class and M-tile height, plus the accelerated
+  // last mode.  The M-tile (64 or 128 output rows) is the one that wastes fewer rows. ----
+  using PlanKey = std::tuple<int, int, int>;   // (mode, or N for the accelerated point; BN; BM)
+  std::map<PlanKey, BatchedContraction> plans;
   struct PlansGuard {
-    std::map<std::pair<int, int>, BatchedContraction> *m;
+    std::map<PlanKey, BatchedContraction> *m;
     ~PlansGuard() {
       for (auto &kv : *m) kv.second.release();
     }
   } pguard{&plans};
+  auto bm_choice = [](int64_t Q) {
+    const int64_t w64 = (Q + 63) / 64 * 64 - Q, w128 = (Q + 127) / 128 * 128 - Q;
+    return w64 < w128 ? 64 : 128;
+  };
   auto build_plans = [&](int target) -> int {
     for (int n = 0; n <= N; ++n) {
       const int mode = n < N ? n : N - 1;
-      std::map<int, std::vector<int>> cls;
-      for (int i = 0; i < n_inst; ++i) cls[bn_class(desc[i].R)].push_back(i);
+      std::map<std::pair<int, int>, std::vector<int>> cls;
+      for (int i = 0; i < n_inst; ++i) {
+        const Contraction c = mttkrp_contraction(T[i], desc[i].fac, mode);
+        cls[{bn_class(desc[i].R), bm_choice(c.Q)}].push_back(i);
+      }
       for (auto &kv : cls) {
         std::vector<const ptg_tensor *> ts;
         std::vector<Contraction> cs;
@@ -608,14 +608,15 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
           outs.push_back(desc[i].M);
           ids.push_back(i);
         }
-        PTG_TRY(batched_plan(ctx, ts, cs, ranks, outs, ids, kv.first, target, &plans[{n, kv.first}]));
+        PTG_TRY(batched_plan(ctx, ts, cs, ranks, outs, ids, kv.first.first, kv.first.second, target,
+                             &plans[PlanKey{n, kv.first.first, kv.first.second}]));
       }
     }
     return PTG_OK;
   };
   auto mttkrp_all = [&](int n, const int *flags) -> int {
     for (auto &kv : plans)
-      if (kv.first.first == n) PTG_TRY(batched_launch(ctx, kv.second, flags, S));
+      if (std::get<0>(kv.first) == n) PTG_TRY(batched_launch(ctx, kv.second, flags, S));
     return PTG_OK;
   };
   // autotuner: time the mode-0..N-1 MTTKRP lists for each candidate CTA target, keep the best
@@ -652,6 +653,29 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
     }
     PTG_TRY(build_plans(best));
   }
+  if (ctx->stats.enabled) {   // one timed pass of the tuned lists (every mode of every instance)
+    double bytes = 0.0;
+    for (int i = 0; i < n_inst; ++i)
+      for (int n = 0; n < N; ++n) {
+        bytes += 4.0 * (double)Tst[i].numel_padded;
+        for (int k = 0; k < N; ++k) bytes += 4.0 * (double)inst[i].dims[k] * inst[i].rank;
+      }
+    cudaEvent_t e0, e1;
+    PTG_CUDA(cudaEventCreate(&e0));
+    PTG_CUDA(cudaEventCreate(&e1));
+    const long long l0 = ctx->stats.launches;
+    PTG_CUDA(cudaEventRecord(e0, S));
+    for (int n = 0; n < N; ++n) PTG_TRY(mttkrp_all(n, nullptr));
+    PTG_CUDA(cudaEventRecord(e1, S));
+    PTG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    PTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->stats.batch_pass_launches = ctx->stats.launches - l0;
+    ctx->stats.batch_pass_ms = ms;
+    ctx->stats.batch_pass_bytes = bytes;
+  }
 
   // ---- initial Grams and cost ----
   PTG_TRY(launch_batched_op(ctx, BatchedOp::Gram, d_desc, n_inst, nullptr, nullptr, S));
@@ -672,6 +696,8 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   // ---- the sweep as a CUDA graph: for each mode, eigenbounds, MTTKRP, NNLS ----
   GraphHolder sweep_graph, accel_graph;
   PTG_CUDA(cudaMemcpyAsync(d_flags, h_flags, sizeof(int) * 4 * n_inst, cudaMemcpyHostToDevice, S));
+  // kernels inside a graph are counted once per replay, not at capture
+  long long cap0 = ctx->stats.launches;
   PTG_CUDA(cudaStreamBeginCapture(S, cudaStreamCaptureModeThreadLocal));
   int cap_rc = PTG_OK;
   for (int n = 0; n < N && cap_rc == PTG_OK; ++n) {
@@ -686,7 +712,10 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   if (cap_rc != PTG_OK) return cap_rc;
   if (ce != cudaSuccess) return cuda_error(ce, "cudaStreamEndCapture(sweep)", __FILE__, __LINE__);
   PTG_CUDA(cudaGraphInstantiate(&sweep_graph.e, sweep_graph.g, 0));
+  const long long sweep_kernels = ctx->stats.launches - cap0;
+  ctx->stats.launches = cap0;
   // acceleration evaluation: combine, Grams, last-mode MTTKRP, cost terms (for flagged instances)
+  cap0 = ctx->stats.launches;
   PTG_CUDA(cudaStreamBeginCapture(S, cudaStreamCaptureModeThreadLocal));
   cap_rc = launch_batched_op(ctx, BatchedOp::AccelCombine, d_desc, n_inst, d_accel, d_step, S);
   if (cap_rc == PTG_OK) cap_rc = launch_batched_op(ctx, BatchedOp::GramAcc, d_desc, n_inst, d_accel, nullptr, S);
@@ -697,6 +726,8 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   if (cap_rc != PTG_OK) return cap_rc;
   if (ce != cudaSuccess) return cuda_error(ce, "cudaStreamEndCapture(accel)", __FILE__, __LINE__);
   PTG_CUDA(cudaGraphInstantiate(&accel_graph.e, accel_graph.g, 0));
+  const long long accel_kernels = ctx->stats.launches - cap0;
+  ctx->stats.launches = cap0;
 
   const int last = N - 1;
   int n_active = n_inst;
@@ -704,7 +735,7 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   for (int sweep = 1; n_active > 0; ++sweep) {
     PTG_CUDA(cudaMemcpyAsync(d_flags, h_flags, sizeof(int) * n_inst, cudaMemcpyHostToDevice, S));
     PTG_CUDA(cudaGraphLaunch(sweep_graph.e, S));
-    count_launches(ctx, 1);
+    count_launches(ctx, (int)sweep_kernels);
     PTG_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(double) * 2 * n_inst * N, cudaMemcpyDeviceToHost, S));
     PTG_CUDA(cudaMemcpyAsync(h_iscal, d_iscal, sizeof(int) * 2 * n_inst * N, cudaMemcpyDeviceToHost, S));
     if (opt.normalization) PTG_TRY(launch_batched_op(ctx, BatchedOp::Normalize, d_desc, n_inst, d_active, nullptr, S));
@@ -747,7 +778,7 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
       PTG_CUDA(cudaMemcpyAsync(d_flags, h_flags, sizeof(int) * 4 * n_inst, cudaMemcpyHostToDevice, S));
       PTG_CUDA(cudaMemcpyAsync(d_step, h_step, sizeof(float) * n_inst, cudaMemcpyHostToDevice, S));
       PTG_CUDA(cudaGraphLaunch(accel_graph.e, S));
-      count_launches(ctx, 1);
+      count_launches(ctx, (int)accel_kernels);
       PTG_CUDA(cudaMemcpyAsync(h_cost, d_cost, sizeof(double) * 2 * n_inst, cudaMemcpyDeviceToHost, S));
       PTG_CUDA(cudaStreamSynchronize(S));
       for (int i = 0; i < n_inst; ++i) {

@@ -48,6 +48,8 @@ struct ptg_ctx_stats {
   double mttkrp_ms = 0.0, mttkrp_bytes = 0.0, mttkrp_flops = 0.0;
   long long tc_launches = 0;
   double tc_ms = 0.0, tc_bytes = 0.0;
+  long long batch_pass_launches = 0;
+  double batch_pass_ms = 0.0, batch_pass_bytes = 0.0;
   struct Pending {
     cudaEvent_t a, b;
     bool tc;
@@ -140,18 +142,18 @@ int check_device_error(ptg_ctx *ctx);
 
 // A batch of MTTKRP-shaped contractions (one per instance, same layout class, FP32
 // storage) planned once into a device work list of (member, m-tile, K-split) items; all
-// members run in one launch, then one launch sums each member's split partials.  Pointers
+// members run in one launch, whose last split per output tile sums the partials.  Pointers
 // are fixed at planning time, so a launch can be captured in a CUDA graph.
 struct BatchedContraction {
   void *mem = nullptr;                 // one allocation: params, items, reduce descriptors, partials
   void *params = nullptr, *items = nullptr, *reduce = nullptr;
-  int nitems = 0, nmembers = 0, BN = 0;
+  int nitems = 0, nmembers = 0, BN = 0, BM = 128;
   bool mmajor = false;
   void release();
 };
 int batched_plan(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, const std::vector<Contraction> &cs,
                  const std::vector<int> &ranks, const std::vector<float *> &outs, const std::vector<int> &insts,
-                 int bn, int target_per_sm, BatchedContraction *bc);
+                 int bn, int bm, int target_per_sm, BatchedContraction *bc);
 // active[inst] == 0 skips that instance's items (nullptr: all run).
 int batched_launch(ptg_ctx *ctx, const BatchedContraction &bc, const int *active, cudaStream_t stream);
 

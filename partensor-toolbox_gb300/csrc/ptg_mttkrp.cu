@@ -90,19 +90,19 @@ template <int BN>
 struct Cfg;
 template <>
 struct Cfg<16> {
-  static constexpr int TN = 4, TM = 4, BM = 128;
+  static constexpr int TN = 4, BM = 128;
 };
 template <>
 struct Cfg<32> {
-  static constexpr int TN = 4, TM = 8, BM = 128;
+  static constexpr int TN = 4, BM = 128;
 };
 template <>
 struct Cfg<64> {
-  static constexpr int TN = 8, TM = 8, BM = 128;
+  static constexpr int TN = 8, BM = 128;
 };
 template <>
 struct Cfg<128> {
-  static constexpr int TN = 8, TM = 8, BM = 64;
+  static constexpr int TN = 8, BM = 64;
 };
 
 constexpr int kThreads = 128;
@@ -110,11 +110,15 @@ constexpr int BK = 32;
 
 // MMAJOR: mode-0 style (P == 1): q contiguous; tile [BK s][BM q]  -> Xs[k][m]
 // KMAJOR: P > 1: p contiguous within (q, s); tile [BM q][BK p]   -> Xs[m][k]
-template <typename T, int BN, bool MMAJOR>
+// BMO: M-tile height (0: the configuration's default); TM follows from the 128 threads.
+template <typename T, int BN, bool MMAJOR, int BMO = 0>
 __device__ __forceinline__ void mttkrp_simt_body(const SimtParams &prm, int mtile, int split) {
   using C = Cfg<BN>;
-  constexpr int BM = C::BM, TM = C::TM, TN = C::TN;
+  constexpr int TN = C::TN;
   constexpr int NG = BN / TN;  // column groups
+  constexpr int BM = BMO ? BMO : C::BM;
+  constexpr int TM = BM * NG / kThreads;
+  static_assert(TM == 2 || TM % 4 == 0, "row tiling");
   static_assert(NG * (BM / TM) == kThreads, "thread tiling");
   constexpr int EV = Vec<T>::kElems;                   // elements per 16-byte load
   constexpr int XLD = MMAJOR ? (BM + 4) : (BK + 4);    // smem row stride (floats)
@@ -229,10 +233,15 @@ __device__ __forceinline__ void mttkrp_simt_body(const SimtParams &prm, int mtil
 #pragma unroll 4
       for (int k = 0; k < BK; ++k) {
         float a[TM], b[TN];
+        if constexpr (TM == 2) {
+          const float2 v = *reinterpret_cast<const float2 *>(xs + k * XLD + mg * TM);
+          a[0] = v.x; a[1] = v.y;
+        } else {
 #pragma unroll
-        for (int i = 0; i < TM; i += 4) {
-          const float4 v = *reinterpret_cast<const float4 *>(xs + k * XLD + mg * TM + i);
-          a[i] = v.x; a[i + 1] = v.y; a[i + 2] = v.z; a[i + 3] = v.w;
+          for (int i = 0; i < TM; i += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(xs + k * XLD + mg * TM + i);
+            a[i] = v.x; a[i + 1] = v.y; a[i + 2] = v.z; a[i + 3] = v.w;
+          }
         }
 #pragma unroll
         for (int j = 0; j < TN; j += 4) {
@@ -341,9 +350,10 @@ KrDev to_dev(const KrSide &s) {
 }
 
 template <int BN>
-size_t simt_smem_bytes(bool mmajor) {
+size_t simt_smem_bytes(bool mmajor, int bm = 0) {
   using Cf = Cfg<BN>;
-  const size_t xrows = mmajor ? BK : Cf::BM, xld = mmajor ? (Cf::BM + 4) : (BK + 4);
+  const size_t BMv = bm ? bm : Cf::BM;
+  const size_t xrows = mmajor ? BK : BMv, xld = mmajor ? (BMv + 4) : (BK + 4);
   return sizeof(float) * (2 * xrows * xld + 2 * BK * BN);
 }
 
@@ -505,46 +515,55 @@ int simt_mttkrp_fixed_scratch(const ptg_tensor *t, const Contraction &c, int R, 
 
 namespace {
 
-template <int BN, bool MMAJOR>
-__global__ void __launch_bounds__(kThreads)
-mttkrp_simt_batched_kernel(const SimtParams *__restrict__ prms, const int4 *__restrict__ items,
-                           const int *__restrict__ active) {
-  const int4 it = items[blockIdx.x];   // (member, m-tile, split, instance)
-  if (active && !active[it.w]) return;
-  mttkrp_simt_body<float, BN, MMAJOR>(prms[it.x], it.y, it.z);
-}
-
 struct ReduceDesc {
-  const float *partial;
-  float *out;
+  const float *partial;   // [nsplit][Q][BN]
+  float *out;             // row-major [q_write][R]
+  unsigned *tickets;      // one per m-tile, zero between launches
   int64_t Q, q_write;
   int nsplit, BN, R, inst;
 };
 
-__global__ void batched_reduce_kernel(const ReduceDesc *__restrict__ d, const int *__restrict__ active) {
-  const ReduceDesc r = d[blockIdx.x];
-  if (active && !active[r.inst]) return;
-  const int64_t n = r.q_write * r.R;
-  for (int64_t idx = threadIdx.x; idx < n; idx += blockDim.x) {
-    const int64_t q = idx / r.R;
-    const int c = (int)(idx % r.R);
+// Work-list MTTKRP: item = (member, m-tile, K-split, instance).  Every split writes its
+// partial tile; the last split of an m-tile to finish (ticket) sums the partials in split
+// order (deterministic) into the member's output and re-arms the ticket.
+template <int BN, bool MMAJOR, int BMV>
+__global__ void __launch_bounds__(kThreads)
+mttkrp_simt_batched_kernel(const SimtParams *__restrict__ prms, const int4 *__restrict__ items,
+                           const ReduceDesc *__restrict__ red, const int *__restrict__ active) {
+  const int4 it = items[blockIdx.x];   // (member, m-tile, split, instance)
+  if (active && !active[it.w]) return;
+  mttkrp_simt_body<float, BN, MMAJOR, BMV>(prms[it.x], it.y, it.z);
+  __shared__ bool last;
+  const ReduceDesc &r = red[it.x];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&r.tickets[it.y], 1u) == (unsigned)(r.nsplit - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const int64_t q0 = (int64_t)it.y * BMV;
+  const int64_t q1 = min(q0 + (int64_t)BMV, r.q_write);
+  const int R = r.R;
+  for (int64_t idx = threadIdx.x; idx < (q1 - q0) * R; idx += kThreads) {
+    const int64_t q = q0 + idx / R;
+    const int c = (int)(idx % R);
     float s = 0.0f;
-    for (int sp = 0; sp < r.nsplit; ++sp) s += r.partial[((int64_t)sp * r.Q + q) * r.BN + c];
-    r.out[q * r.R + c] = s;
+    for (int sp = 0; sp < r.nsplit; ++sp) s += __ldcg(&r.partial[((int64_t)sp * r.Q + q) * BN + c]);
+    r.out[q * R + c] = s;
   }
+  if (threadIdx.x == 0) r.tickets[it.y] = 0u;
 }
 
 template <int BN>
 int batched_plan_bn(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, const std::vector<Contraction> &cs,
                     const std::vector<int> &ranks, const std::vector<float *> &outs, const std::vector<int> &insts,
-                    int target_per_sm, BatchedContraction *bc) {
-  using Cf = Cfg<BN>;
+                    int bm, int target_per_sm, BatchedContraction *bc) {
   const size_t m = cs.size();
   std::vector<SimtParams> prms(m);
   std::vector<int4> items;
   std::vector<ReduceDesc> red(m);
-  std::vector<size_t> part_off(m);
-  size_t part_total = 0;
+  std::vector<size_t> part_off(m), tick_off(m);
+  size_t part_total = 0, tick_total = 0;
   // total work, to size every member's split count in proportion to its share
   double work_total = 0.0;
   for (size_t i = 0; i < m; ++i) work_total += (double)cs[i].P * cs[i].Q * cs[i].S;
@@ -573,7 +592,7 @@ int batched_plan_bn(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, con
       prm.pblocks = (c.P + BK - 1) / BK;
       prm.ktiles_total = c.S * prm.pblocks;
     }
-    const int64_t mtiles = (c.Q + Cf::BM - 1) / Cf::BM;
+    const int64_t mtiles = (c.Q + bm - 1) / bm;
     const double share = ((double)c.P * c.Q * c.S) / work_total * target_ctas;
     int64_t nsplit = std::max<int64_t>(1, (int64_t)(share / (double)mtiles + 0.5));
     nsplit = std::min<int64_t>(nsplit, prm.ktiles_total);
@@ -582,15 +601,17 @@ int batched_plan_bn(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, con
     prm.nsplit = (int)std::max<int64_t>(nsplit, 2);   // always through the partials
     part_off[i] = part_total;
     part_total += (size_t)nsplit * c.Q * BN;
+    tick_off[i] = tick_total;
+    tick_total += (size_t)mtiles;
     for (int64_t mt = 0; mt < mtiles; ++mt)
       for (int64_t sp = 0; sp < nsplit; ++sp) items.push_back(make_int4((int)i, (int)mt, (int)sp, insts[i]));
-    red[i] = ReduceDesc{nullptr, outs[i], c.Q, c.q_write, (int)nsplit, BN, ranks[i], insts[i]};
+    red[i] = ReduceDesc{nullptr, outs[i], nullptr, c.Q, c.q_write, (int)nsplit, BN, ranks[i], insts[i]};
   }
   bc->release();
-  const size_t a1 = (sizeof(SimtParams) * m + 255) / 256 * 256;
-  const size_t a2 = (sizeof(int4) * items.size() + 255) / 256 * 256;
-  const size_t a3 = (sizeof(ReduceDesc) * m + 255) / 256 * 256;
-  cudaError_t e = cudaMalloc(&bc->mem, a1 + a2 + a3 + sizeof(float) * part_total + 256);
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t a1 = up(sizeof(SimtParams) * m), a2 = up(sizeof(int4) * items.size()),
+               a3 = up(sizeof(ReduceDesc) * m), a4 = up(sizeof(unsigned) * tick_total);
+  cudaError_t e = cudaMalloc(&bc->mem, a1 + a2 + a3 + a4 + sizeof(float) * part_total + 256);
   if (e != cudaSuccess) {
     bc->mem = nullptr;
     return cuda_error(e, "cudaMalloc(batched plan)", __FILE__, __LINE__);
@@ -599,20 +620,24 @@ int batched_plan_bn(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, con
   SimtParams *d_prm = (SimtParams *)b;
   int4 *d_items = (int4 *)(b + a1);
   ReduceDesc *d_red = (ReduceDesc *)(b + a1 + a2);
-  float *d_part = (float *)(b + a1 + a2 + a3);
+  unsigned *d_tick = (unsigned *)(b + a1 + a2 + a3);
+  float *d_part = (float *)(b + a1 + a2 + a3 + a4);
   for (size_t i = 0; i < m; ++i) {
     prms[i].partial = d_part + part_off[i];
     red[i].partial = d_part + part_off[i];
+    red[i].tickets = d_tick + tick_off[i];
   }
   PTG_CUDA(cudaMemcpy(d_prm, prms.data(), sizeof(SimtParams) * m, cudaMemcpyHostToDevice));
   PTG_CUDA(cudaMemcpy(d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice));
   PTG_CUDA(cudaMemcpy(d_red, red.data(), sizeof(ReduceDesc) * m, cudaMemcpyHostToDevice));
+  PTG_CUDA(cudaMemset(d_tick, 0, sizeof(unsigned) * std::max<size_t>(tick_total, 1)));
   bc->params = d_prm;
   bc->items = d_items;
   bc->reduce = d_red;
   bc->nitems = (int)items.size();
   bc->nmembers = (int)m;
   bc->BN = BN;
+  bc->BM = bm;
   bc->mmajor = mmajor;
   return PTG_OK;
 }
@@ -627,35 +652,37 @@ void BatchedContraction::release() {
 
 int batched_plan(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, const std::vector<Contraction> &cs,
                  const std::vector<int> &ranks, const std::vector<float *> &outs, const std::vector<int> &insts,
-                 int bn, int target_per_sm, BatchedContraction *bc) {
+                 int bn, int bm, int target_per_sm, BatchedContraction *bc) {
   if (cs.empty()) return PTG_OK;
   for (const ptg_tensor *t : ts)
     if (t->dtype != PTG_F32) return set_error(PTG_ERR_UNSUPPORTED, "batched MTTKRP: FP32 storage only");
   const bool mm = cs[0].P == 1;
   for (const Contraction &c : cs)
     if ((c.P == 1) != mm) return set_error(PTG_ERR_INVALID, "internal: mixed layouts in one batch");
-  if (bn == 16) return batched_plan_bn<16>(ctx, ts, cs, ranks, outs, insts, target_per_sm, bc);
-  if (bn == 32) return batched_plan_bn<32>(ctx, ts, cs, ranks, outs, insts, target_per_sm, bc);
-  if (bn == 64) return batched_plan_bn<64>(ctx, ts, cs, ranks, outs, insts, target_per_sm, bc);
+  if (bm != 64 && bm != 128) return set_error(PTG_ERR_INVALID, "internal: batched M-tile must be 64 or 128");
+  if (bn == 16) return batched_plan_bn<16>(ctx, ts, cs, ranks, outs, insts, bm, target_per_sm, bc);
+  if (bn == 32) return batched_plan_bn<32>(ctx, ts, cs, ranks, outs, insts, bm, target_per_sm, bc);
+  if (bn == 64) return batched_plan_bn<64>(ctx, ts, cs, ranks, outs, insts, bm, target_per_sm, bc);
   return set_error(PTG_ERR_UNSUPPORTED, "batched MTTKRP: rank > 64");
+}
+
+template <int BNV, bool MM, int BMV>
+static int batched_launch_t(const BatchedContraction &bc, const int *active, cudaStream_t stream) {
+  auto kern = mttkrp_simt_batched_kernel<BNV, MM, BMV>;
+  const size_t smem = simt_smem_bytes<BNV>(MM, BMV);
+  PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<bc.nitems, kThreads, smem, stream>>>((const SimtParams *)bc.params, (const int4 *)bc.items,
+                                              (const ReduceDesc *)bc.reduce, active);
+  PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
 }
 
 template <int BNV>
 static int batched_launch_bn(const BatchedContraction &bc, const int *active, cudaStream_t stream) {
-  const SimtParams *p = (const SimtParams *)bc.params;
-  const int4 *it = (const int4 *)bc.items;
-  const size_t smem = simt_smem_bytes<BNV>(bc.mmajor);
-  if (bc.mmajor) {
-    PTG_CUDA(cudaFuncSetAttribute(mttkrp_simt_batched_kernel<BNV, true>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    mttkrp_simt_batched_kernel<BNV, true><<<bc.nitems, kThreads, smem, stream>>>(p, it, active);
-  } else {
-    PTG_CUDA(cudaFuncSetAttribute(mttkrp_simt_batched_kernel<BNV, false>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    mttkrp_simt_batched_kernel<BNV, false><<<bc.nitems, kThreads, smem, stream>>>(p, it, active);
-  }
-  PTG_CUDA(cudaGetLastError());
-  return PTG_OK;
+  if (bc.mmajor) return bc.BM == 64 ? batched_launch_t<BNV, true, 64>(bc, active, stream)
+                                    : batched_launch_t<BNV, true, 128>(bc, active, stream);
+  return bc.BM == 64 ? batched_launch_t<BNV, false, 64>(bc, active, stream)
+                     : batched_launch_t<BNV, false, 128>(bc, active, stream);
 }
 
 int batched_launch(ptg_ctx *ctx, const BatchedContraction &bc, const int *active, cudaStream_t stream) {
@@ -663,9 +690,7 @@ int batched_launch(ptg_ctx *ctx, const BatchedContraction &bc, const int *active
   if (bc.BN == 16) PTG_TRY(batched_launch_bn<16>(bc, active, stream));
   else if (bc.BN == 32) PTG_TRY(batched_launch_bn<32>(bc, active, stream));
   else PTG_TRY(batched_launch_bn<64>(bc, active, stream));
-  batched_reduce_kernel<<<bc.nmembers, 256, 0, stream>>>((const ReduceDesc *)bc.reduce, active);
-  PTG_CUDA(cudaGetLastError());
-  count_launches(ctx, 2);
+  count_launches(ctx, 1);
   return PTG_OK;
 }
 

@@ -441,11 +441,18 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   }
   __syncthreads();
 
-  int it = 0;
-  for (;;) {
-    // grad = Y Z~ - W~ ; stop-test partials
-    float g[ROWS][RB];
-    float mx = 0.0f, mn = INFINITY;
+  // Global stop test without a reduction: the test of include/NesterovMNLS.hpp:217-218
+  // (max |grad .* Y| <= delta1 and min grad >= -delta2) fails iff some element violates it,
+  // so each warp that sees a violation writes 1 into a flag word of iteration `it` in CTA 0's
+  // shared memory (three words used in rotation).  One split cluster barrier per iteration:
+  // arrive after the flag write and the speculative update, wait after the next gradient, so
+  // the barrier's latency hides behind that product.  The update of iteration `it` keeps A_it
+  // in the staging rows (As) in case the flag says stop.
+  int *vflag0 = cluster.map_shared_rank(flags + 1, 0);
+  if (tid < 3) flags[1 + tid] = 0;
+  cluster.sync();
+  float g[ROWS][RB];
+  auto gradient = [&]() {   // grad = Y Z~ - W~
 #pragma unroll
     for (int j = 0; j < ROWS; ++j)
 #pragma unroll
@@ -462,59 +469,42 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
         for (int b = 0; b < RB; ++b) g[j][b] = fmaf(yk, z[b], g[j][b]);
       }
     }
+  };
+  gradient();
+  int it = 0;
+  for (;;) {
+    if (it >= kMaxInner) break;   // A_it is the result
+    bool viol = false;
 #pragma unroll
     for (int j = 0; j < ROWS; ++j) {
       const bool rowok = (gw + j * stride) < I;
 #pragma unroll
       for (int b = 0; b < RB; ++b)
-        if (rowok && colok[b]) {
-          mx = fmaxf(mx, fabsf(g[j][b] * Y[j][b]));
-          mn = fminf(mn, g[j][b]);
-        }
+        if (rowok && colok[b]) viol |= (fabsf(g[j][b] * Y[j][b]) > a.delta1) || (g[j][b] < -a.delta2);
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-    }
-    if (lane == 0) {
-      wred[2 * warp] = mx;
-      wred[2 * warp + 1] = mn;
-    }
-    __syncthreads();
-    if (warp == 0) {   // max/min are exact in FP32, so the reduction order does not matter
-      float M1 = lane < kNnlsWarps ? wred[2 * lane] : 0.0f;
-      float M2 = lane < kNnlsWarps ? wred[2 * lane + 1] : INFINITY;
-      for (int o = 8; o > 0; o >>= 1) {
-        M1 = fmaxf(M1, __shfl_xor_sync(0xffffffffu, M1, o));
-        M2 = fminf(M2, __shfl_xor_sync(0xffffffffu, M2, o));
-      }
-      if (lane == 0) {
-        slots[2 * (it & 1)] = M1;
-        slots[2 * (it & 1) + 1] = M2;
-      }
-    }
-    cluster.sync();
-    float gmx = 0.0f, gmn = INFINITY;
-    if (lane < CS) {
-      const float *rs = cluster.map_shared_rank(slots, lane);
-      gmx = rs[2 * (it & 1)];
-      gmn = rs[2 * (it & 1) + 1];
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      gmx = fmaxf(gmx, __shfl_xor_sync(0xffffffffu, gmx, o));
-      gmn = fminf(gmn, __shfl_xor_sync(0xffffffffu, gmn, o));
-    }
-    // stop test of include/NesterovMNLS.hpp:217-218
-    if ((gmx <= a.delta1 && gmn >= -a.delta2) || it >= kMaxInner) break;
+    if (__any_sync(0xffffffffu, viol) && lane == 0) *(volatile int *)&vflag0[it % 3] = 1;
+    if (rank == 0 && tid == 0) flags[1 + (it + 1) % 3] = 0;   // the word of it+1 (read last at it-2)
     const float beta = np->beta[it];
 #pragma unroll
     for (int j = 0; j < ROWS; ++j)
 #pragma unroll
       for (int b = 0; b < RB; ++b) {
+        if (colok[b]) As[(warp * ROWS + j) * R + lane + 32 * b] = Ac[j][b];   // A_it
         const float na = fmaxf(Y[j][b] - g[j][b] * invL, 0.0f);       // :220
         Y[j][b] = (1.0f + beta) * na - beta * Ac[j][b];                 // :228
         Ac[j][b] = na;
       }
+    asm volatile("barrier.cluster.arrive.release;" ::: "memory");
+    gradient();   // of it+1 (discarded if it stops at it)
+    asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
+    if (*(volatile int *)&vflag0[it % 3] == 0) {   // no violation: stop, the result is A_it
+#pragma unroll
+      for (int j = 0; j < ROWS; ++j)
+#pragma unroll
+        for (int b = 0; b < RB; ++b)
+          if (colok[b]) Ac[j][b] = As[(warp * ROWS + j) * R + lane + 32 * b];
+      break;
+    }
     ++it;
   }
 

@@ -143,3 +143,16 @@ def test_cpd_dimtree_3way(pkg, ctx):
     st = pkg.cpdDimTree(X, 4, pkg.Options(order=3, max_iter=10), init, ctx=ctx)
     ref = oc.cpd_dimtree_als(X, 4, oc.Options(order=3, max_iter=10), init)
     assert abs(st.rel_costFunction - ref.rel_costFunction) < 1e-4
+
+
+def test_cpd_bf16_verify_fp32_reports_fp32_cost(pkg, ctx):
+    """verify_fp32: after a BF16 main loop the reported cost is the final factors' cost on the
+    FP32 copy (one MTTKRP), so it equals the FP64 residual of the returned factors."""
+    X, A, init = _cfg1_like((48, 40, 36), 6, seed=6, snr_db=30.0)
+    st = pkg.cpd(X, 6, pkg.Options(order=3, max_iter=12, precision="bf16", verify_fp32=True), init, ctx=ctx)
+    assert st.refine_sweeps_done == 0
+    assert oc.cost_from_factors(X, st.factors) == pytest.approx(st.f_value, rel=1e-5)
+    plain = pkg.cpd(X, 6, pkg.Options(order=3, max_iter=12, precision="bf16"), init, ctx=ctx)
+    # the same factors; only where the cost is measured differs
+    for k in range(3):
+        assert np.array_equal(st.factors[k], plain.factors[k])
