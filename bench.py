@@ -441,6 +441,167 @@ def run_batch_ours(args):
     ctx.close()
 
 
+def run_dimtree(args):
+    """160^4, R=64, collinear factors (cosine 0.6, seed 3), 25 dB: cpdDimTree to the target
+    (noise floor + 1e-3) on BF16 tcgen05 storage with the fit verified on FP32, beside the
+    plain FP32 dimension tree, the direct (non-tree) BF16 solve and the learned warm start."""
+    import numpy as np
+    import torch
+    ws, rank = _dist()
+    torch.cuda.set_device(0)
+    ge = __import__("__graft_entry__")
+    pkg = ge.load_package()
+    from partensor_toolbox_gb300 import datagen as dg
+    dims, R = [160, 160, 160, 160], 64
+    p = dg.make_cpd_problem(dims, R, seed=3, init_seed=4, snr_db=25.0, collinearity=0.6, device="cuda")
+    target = p.noise_rel + 1e-3
+    init = [f.cpu().numpy() for f in p.init_factors]
+    ctx = pkg.Context(0)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    Xb = pkg.Tensor(ctx, (p.X.data_ptr(), dims), precision="bf16")
+    Xf = pkg.Tensor(ctx, (p.X.data_ptr(), dims), precision="f32")
+    mi = args.max_iter
+
+    def run(form, dimtree=True, warm=False):
+        kw = dict(order=4, max_iter=mi, threshold_error=target)
+        if form == "bf16":
+            kw.update(precision="bf16", verify_fp32=True)
+        if warm:
+            kw.update(warm_start=True, warm_model=pkg.WarmStartModel(ctx, R, seed=7), warm_log_sweeps=5,
+                      warm_train_steps=300)
+        o = pkg.Options(**kw)
+        X = Xb if form == "bf16" else Xf
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        st = pkg.cpd_resident(ctx, X, R, o, init, refine=Xf if form == "bf16" else None, dimtree=dimtree)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t, st
+
+    for _ in range(max(1, args.warmup)):
+        run("f32")
+    res = {}
+    ctx.enable_stats(True)
+    clk = ClockSampler()
+    clk.start()
+    for name, form, dt, warm in [("dimtree_f32", "f32", True, False), ("direct_f32", "f32", False, False),
+                                 ("dimtree_f32_warm", "f32", True, True), ("dimtree_bf16", "bf16", True, False)]:
+        ts, st = [], None
+        ctx.reset_stats()
+        for _ in range(max(1, args.steps if name == "dimtree_f32" else 1)):
+            t, st = run(form, dt, warm)
+            ts.append(t)
+        kst = ctx.stats()
+        res[name] = {"seconds": statistics.mean(ts), "sweeps": st.ao_iter, "final_rel_err": st.rel_costFunction,
+                     "converged": bool(st.rel_costFunction <= target),
+                     "nesterov_iters_total": st.nesterov_iters_total,
+                     "nesterov_iters_after_sweep5": int(sum(sum(t["nesterov_iters"]) for t in st.trace[5:])),
+                     "gpu_launches": kst["launches"] // max(1, len(ts)),
+                     "ms_per_sweep": 1e3 * statistics.mean(ts) / max(1, st.ao_iter),
+                     "mttkrp_ms_per_sweep": kst["mttkrp_ms"] / max(1, len(ts)) / max(1, st.ao_iter)}
+        if name == "dimtree_f32":
+            tc = kst
+    clocks = clk.stop()
+    ach = tc["mttkrp_bytes"] / (tc["mttkrp_ms"] * 1e-3) / 1e9 if tc["mttkrp_ms"] > 0 else None
+    cpu = None
+    if not args.no_cpu:
+        Xh = p.X.cpu().numpy()
+        threads = os.cpu_count() or 1
+        s_sweep, _ = cpu_sweep_seconds(Xh, dims, R, init, threads)
+        sw = res["dimtree_f32"]["sweeps"]
+        cpu = {"value": s_sweep * sw, "unit": "s", "cores": threads, "kind": "port",
+               "sample": f"1 full-size FP64 ALS sweep of the OpenMP restatement of CpdOpenMP (oracle/cpd_omp.c, "
+                         f"direct MTTKRP, no dimension tree) = {s_sweep:.2f} s, x {sw} sweeps"}
+        del Xh
+    peak, peak_kind = _peaks()
+    line = {"metric": "time to rel. fit err <= noise floor + 1e-3, 160^4 R=64 collinear nonneg cpdDimTree (FP32)",
+            "value": res["dimtree_f32"]["seconds"], "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": False, "dtype": "f32",
+            "data": "synthetic (U[0,1] factors with a shared component, cosine 0.6, seed 3; 25 dB)",
+            "config": {"workload": "cpdDimTree 160x160x160x160 R=64", "target_rel": target,
+                       "noise_floor_rel": p.noise_rel, "max_iter": mi},
+            "runs": res, "cpu_baseline": cpu,
+            "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                         "frac": (ach / peak) if ach else None, "peak_kind": peak_kind,
+                         "kernel": "MTTKRP contractions of the FP32 dimension tree (node contractions, leaves, "
+                                   "acceleration cost), summed event time",
+                         "launches": tc["mttkrp_launches"]},
+            "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_gtc(args):
+    """50000 x 50000 x 5000, 200 M observed entries sampled uniformly without replacement
+    (seed 5), values from a rank-32 U[0,1] model with 10% relative Gaussian noise; 1% held out.
+    Stochastic GTC (c = 0.01, lambda = 1e-3, R = 32) on device-resident int32 COO + FP32
+    values; reports observed entries/s and the held-out RMSE."""
+    import numpy as np
+    import torch
+    torch.cuda.set_device(0)
+    ge = __import__("__graft_entry__")
+    pkg = ge.load_package()
+    dims, R, total_nnz = [50000, 50000, 5000], 32, int(args.gtc_nnz)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    cells = dims[0] * dims[1] * dims[2]
+    flat = torch.unique(torch.randint(0, cells, (int(total_nnz * 1.001) + 1024,), generator=g, device="cuda"))
+    flat = flat[torch.randperm(flat.numel(), generator=g, device="cuda")][:total_nnz]
+    A = [torch.rand(I, R, generator=g, device="cuda") for I in dims]
+    idx = torch.empty(3, total_nnz, dtype=torch.int32, device="cuda")
+    vals = torch.empty(total_nnz, dtype=torch.float32, device="cuda")
+    clean = torch.empty(total_nnz, dtype=torch.float32, device="cuda")
+    for s in range(0, total_nnz, 1 << 24):
+        f = flat[s:s + (1 << 24)]
+        i0, i1, i2 = f % dims[0], (f // dims[0]) % dims[1], f // (dims[0] * dims[1])
+        idx[0, s:s + f.numel()], idx[1, s:s + f.numel()], idx[2, s:s + f.numel()] = i0, i1, i2
+        v = (A[0][i0] * A[1][i1] * A[2][i2]).sum(1)
+        clean[s:s + f.numel()] = v
+        vals[s:s + f.numel()] = v * (1 + 0.1 * torch.randn(v.shape, generator=g, device="cuda"))
+    del flat
+    n_hold = total_nnz // 100
+    n_train = total_nnz - n_hold
+    idx_tr = idx[:, :n_train].contiguous()
+    vals_tr = vals[:n_train].contiguous()
+    idx_ho, vals_ho, clean_ho = idx[:, n_train:], vals[n_train:], clean[n_train:]
+    ctx = pkg.Context(0)
+    init = [np.random.default_rng(k).random((I, R)) for k, I in enumerate(dims)]
+
+    def rmse(factors):
+        F = [torch.tensor(np.asarray(f), dtype=torch.float32, device="cuda") for f in factors]
+        pred = (F[0][idx_ho[0].long()] * F[1][idx_ho[1].long()] * F[2][idx_ho[2].long()]).sum(1)
+        return float(torch.sqrt(torch.mean((pred - vals_ho) ** 2)))
+
+    out = {}
+    for name, stoch, it in [("stochastic", True, args.gtc_epochs), ("full", False, args.gtc_full_iters)]:
+        o = pkg.SparseOptions(order=3, rank=R, tnsDims=dims, max_iter=it, lambdas=[1e-3] * 3,
+                              c_stochastic_perc=0.01, factorsInit=init, threshold_error=0.0)
+        pkg.gtc_device(idx_tr.data_ptr(), vals_tr.data_ptr(), n_train,
+                       dataclasses_replace(o, max_iter=1), stochastic=stoch, ctx=ctx)   # warm-up
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        st = pkg.gtc_device(idx_tr.data_ptr(), vals_tr.data_ptr(), n_train, o, stochastic=stoch, ctx=ctx)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t
+        passes = st.epochs if stoch else st.ao_iter
+        out[name] = {"seconds": el, "seconds_setup": st.seconds_setup, "ao_iter": st.ao_iter, "epochs": st.epochs,
+                     "observed_entries_per_s": n_train * max(1, passes) / el,
+                     "rel_cost": st.rel_costFunction, "heldout_rmse": rmse(st.factors)}
+    floor = float(torch.sqrt(torch.mean((clean_ho - vals_ho) ** 2)))
+    line = {"metric": "observed entries/s, stochastic GTC 50000x50000x5000, 200M entries, R=32, c=0.01",
+            "value": out["stochastic"]["observed_entries_per_s"], "unit": "entries/s", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic (uniform sample, rank-32 model, 10% noise)",
+            "config": {"workload": "gtc_stochastic 50000x50000x5000", "nnz_train": n_train, "nnz_heldout": n_hold,
+                       "rank": R, "lambda": 1e-3, "c_stochastic_perc": 0.01},
+            "runs": out, "heldout_rmse_noise_floor": floor}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def dataclasses_replace(o, **kw):
+    import dataclasses
+    return dataclasses.replace(o, **kw)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -456,12 +617,20 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--warmup-ref", type=int, default=0)
     ap.add_argument("--sweeps-to-target", type=int, default=20)
-    ap.add_argument("--workload", default="cpd-1000", choices=["cpd-1000", "fmri-batch"],
-                    help="cpd-1000: the headline 1000^3 solve; fmri-batch: 256 small CPDs in one call")
+    ap.add_argument("--workload", default="cpd-1000", choices=["cpd-1000", "fmri-batch", "dimtree-160", "gtc-sparse"],
+                    help="cpd-1000: the headline 1000^3 solve; fmri-batch: 256 small CPDs in one call; "
+                         "dimtree-160: 160^4 R=64 cpdDimTree; gtc-sparse: 200M-entry stochastic completion")
+    ap.add_argument("--gtc-nnz", type=float, default=200e6)
+    ap.add_argument("--gtc-epochs", type=int, default=2, help="stochastic GTC epochs (its max_iter)")
+    ap.add_argument("--gtc-full-iters", type=int, default=2)
     ap.add_argument("--batch-sample", type=int, default=32, help="instances the CPU baseline solves")
     args = ap.parse_args()
     if args.workload == "fmri-batch":
         run_batch_reference(args) if args.impl == "reference" else run_batch_ours(args)
+    elif args.workload == "dimtree-160":
+        run_dimtree(args)
+    elif args.workload == "gtc-sparse":
+        run_gtc(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -34,6 +34,8 @@ struct AlsBuffers {
   NnlsParams *np = nullptr;
   double *dsc = nullptr;  // [N][2]: <M, A>, sum(Z .* G); [N][2..3]: cost terms of a point
   int *isc = nullptr;     // [N][2]: iterations, repaired
+  double *W = nullptr;    // R x R FP64: Z^{-1} or (M^T M)^{-1/2} (other constraints)
+  float *MtM = nullptr;   // R x R FP32 Gram of M (orthogonality)
   void *base = nullptr;
 
   int alloc(const int64_t *dims, int order, int rank, int64_t rows_left = 0, int64_t rows_right = 0) {
@@ -67,6 +69,8 @@ struct AlsBuffers {
     const size_t o_np = take(sizeof(NnlsParams));
     const size_t o_d = take(sizeof(double) * 4 * N);
     const size_t o_i = take(sizeof(int) * 2 * N);
+    const size_t o_W = take(sizeof(double) * R * R);
+    const size_t o_C = take(sizeof(float) * R * R);
     cudaError_t e = cudaMalloc(&base, off);
     if (e != cudaSuccess) {
       base = nullptr;
@@ -87,6 +91,8 @@ struct AlsBuffers {
     np = (NnlsParams *)(b + o_np);
     dsc = (double *)(b + o_d);
     isc = (int *)(b + o_i);
+    W = (double *)(b + o_W);
+    MtM = (float *)(b + o_C);
     return PTG_OK;
   }
   ~AlsBuffers() {
@@ -110,8 +116,11 @@ struct Runner {
     cudaStream_t S = ctx->stream, T = ctx->side;
     const int N = b.N, R = b.R;
     for (int n = 0; n < N; ++n) {
-      if (opt->constraints[n] != PTG_NONNEGATIVITY)
-        return set_error(PTG_ERR_UNSUPPORTED, "only nonnegativity constraints are implemented on the GPU path");
+      const int con = opt->constraints[n];
+      if (con != PTG_NONNEGATIVITY) {
+        PTG_TRY(other_update(X, n));
+        continue;
+      }
       PTG_CUDA(cudaEventRecord(ctx->ev_fork, S));
       PTG_CUDA(cudaStreamWaitEvent(T, ctx->ev_fork, 0));
       PTG_TRY(launch_eigen_bounds(b.gram, N, n, R, b.np, T));
@@ -144,6 +153,47 @@ struct Runner {
     if (!std::isfinite(f2)) return set_error(PTG_ERR_NUMERIC, "cost is NaN or Inf");
     *f_out = std::sqrt(std::max(f2, 0.0));
     for (int n = 0; n < N; ++n) iters[n] = hi[2 * n];
+    return PTG_OK;
+  }
+
+  // the MTTKRP of mode n into b.M (direct or through the dimension-tree nodes)
+  int mode_mttkrp(const ptg_tensor *X, int n) {
+    cudaStream_t S = ctx->stream;
+    if (!dimtree) {
+      Contraction c = mttkrp_contraction(X, b.fac, n);
+      return contraction_launch(ctx, X, c, b.R, b.M, S);
+    }
+    const int h = dimtree_split(b.N);
+    if (n == 0) PTG_TRY(contraction_launch(ctx, X, node_contraction(X, b.fac, true), b.R, b.TL, S));
+    if (n == h) PTG_TRY(contraction_launch(ctx, X, node_contraction(X, b.fac, false), b.R, b.TR, S));
+    return launch_leaf_mttkrp(ctx, X, n < h ? b.TL : b.TR, b.fac, n, b.R, b.M, S);
+  }
+
+  // update_factor for the constraints other than nonnegativity (include/Cpd.hpp:196-222),
+  // then the Gram (:227); the cost terms of the last mode are those of the Gram form
+  int other_update(const ptg_tensor *X, int n) {
+    cudaStream_t S = ctx->stream;
+    const int N = b.N, R = b.R, con = opt->constraints[n];
+    PTG_TRY(mode_mttkrp(X, n));
+    if (con == PTG_UNCONSTRAINED) {
+      PTG_TRY(launch_eigen_bounds(b.gram, N, n, R, b.np, S));   // Z = Hadamard of the other Grams
+      count_launches(ctx, 1);
+      PTG_TRY(launch_update_unconstrained(ctx, b.M, b.fac[n], b.rows[n], R, b.np, b.W, S));
+    } else if (con == PTG_ORTHOGONALITY) {
+      if (b.rows[n] < R) return set_error(PTG_ERR_INVALID, "orthogonality needs I_n >= R");
+      PTG_TRY(launch_gram(b.M, b.rows[n], R, b.MtM, b.gpart, S));
+      count_launches(ctx, 2);
+      PTG_TRY(launch_update_orthogonal(ctx, b.M, b.fac[n], b.rows[n], R, b.MtM, b.W, S));
+    } else if (con != PTG_SPARSITY && con != PTG_CONSTANT) {
+      return set_error(PTG_ERR_INVALID, "unknown constraint");
+    }
+    PTG_TRY(launch_gram(b.fac[n], b.rows[n], R, b.gram[n], b.gpart, S));
+    count_launches(ctx, 2);
+    PTG_CUDA(cudaMemsetAsync(b.isc + 2 * n, 0, 2 * sizeof(int), S));
+    if (n == N - 1) {
+      PTG_TRY(launch_cost_terms(b.M, b.fac[n], b.rows[n], b.gram, N, R, b.dsc + 4 * n, S));
+      count_launches(ctx, 1);
+    }
     return PTG_OK;
   }
 

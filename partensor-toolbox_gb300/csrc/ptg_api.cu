@@ -102,7 +102,8 @@ int check_device_error(ptg_ctx *ctx) {
   if (h != 0) {
     PTG_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
     PTG_CUDA(cudaStreamSynchronize(ctx->stream));
-    return set_error(h, "a device-side bounded wait gave up (kernel returned early)");
+    return set_error(h, h == PTG_ERR_TIMEOUT ? "a device-side bounded wait gave up (kernel returned early)"
+                                             : "a kernel reported a singular or non-finite R x R system");
   }
   return PTG_OK;
 }

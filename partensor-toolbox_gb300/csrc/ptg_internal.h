@@ -202,6 +202,12 @@ int launch_accel_combine(const float *const *cur, const float *const *old, float
                          const int *rows, int order, int R, double step, cudaStream_t stream);
 // out2[0] = <M, A_last> (FP64), out2[1] = sum(Z_last .* G_last) with Z_last the Hadamard
 // of grams[0..order-2].
+// update_factor for unconstrained (A = M Z^{-1}, Z in np->Z) and orthogonal (A = M (M^T M)^{-1/2},
+// MtM the FP32 Gram of M) modes; W is an R x R FP64 scratch.  ptg_constraints.cu.
+int launch_update_unconstrained(ptg_ctx *ctx, const float *M, float *A, int I, int R, const NnlsParams *np,
+                                double *W, cudaStream_t s);
+int launch_update_orthogonal(ptg_ctx *ctx, const float *M, float *A, int I, int R, const float *MtM, double *W,
+                             cudaStream_t s);
 int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const float *const *grams,
                       int order, int R, double *out2, cudaStream_t stream);
 

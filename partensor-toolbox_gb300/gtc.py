@@ -52,16 +52,21 @@ class SparseStatus:
     trace: list = dataclasses.field(default_factory=list)
 
 
-def _run(idx: np.ndarray, vals: np.ndarray, options: SparseOptions, stochastic: bool,
-         ctx: Optional[Context]) -> SparseStatus:
+def _run(idx, vals, options: SparseOptions, stochastic: bool, ctx: Optional[Context],
+         device_ptrs: Optional[tuple] = None) -> SparseStatus:
     ctx = ctx or default_context()
     lib = ctx._lib
     N = options.order
     dims = [int(d) for d in options.tnsDims]
     R = int(options.rank)
-    idx = np.ascontiguousarray(idx, dtype=np.int32)
-    vals = np.ascontiguousarray(vals, dtype=np.float32)
-    nnz = vals.shape[0]
+    if device_ptrs is None:
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        vals = np.ascontiguousarray(vals, dtype=np.float32)
+        nnz = vals.shape[0]
+        p_idx, p_vals, on_dev = idx.ctypes.data_as(ctypes.c_void_p), vals.ctypes.data_as(ctypes.c_void_p), 0
+    else:
+        p_idx, p_vals, nnz = device_ptrs
+        p_idx, p_vals, on_dev = ctypes.c_void_p(int(p_idx)), ctypes.c_void_p(int(p_vals)), 1
     o = GtcOptions()
     lib.ptg_gtc_default_options(N, ctypes.byref(o))
     o.threshold_error = options.threshold_error
@@ -85,8 +90,7 @@ def _run(idx: np.ndarray, vals: np.ndarray, options: SparseOptions, stochastic: 
     res = GtcResult()
     trace = (SweepTrace * options.max_iter)()
     d = (ctypes.c_int64 * N)(*dims)
-    check(lib.ptg_gtc(ctx.handle, N, d, nnz, idx.ctypes.data_as(ctypes.c_void_p),
-                      vals.ctypes.data_as(ctypes.c_void_p), 0, R, ctypes.byref(o), ip, op,
+    check(lib.ptg_gtc(ctx.handle, N, d, int(nnz), p_idx, p_vals, on_dev, R, ctypes.byref(o), ip, op,
                       ctypes.byref(res), trace))
     st = SparseStatus(options=options, factors=outs, frob_tns=res.frob_tns, f_value=res.f_value,
                       rel_costFunction=res.rel_costFunction, ao_iter=res.ao_iter, epochs=res.epochs,
@@ -118,6 +122,12 @@ def gtc_coo(idx: np.ndarray, vals: np.ndarray, options: SparseOptions, stochasti
             ctx: Optional[Context] = None) -> SparseStatus:
     """Same solve from int32 COO indices [N][nnz] and FP32 values (the device-native form)."""
     return _run(idx, vals, options, stochastic, ctx)
+
+
+def gtc_device(idx_dev_ptr: int, vals_dev_ptr: int, nnz: int, options: SparseOptions, stochastic: bool = False,
+               ctx: Optional[Context] = None) -> SparseStatus:
+    """Same solve from device-resident int32 COO indices [N][nnz] and FP32 values (no host copy)."""
+    return _run(None, None, options, stochastic, ctx, device_ptrs=(idx_dev_ptr, vals_dev_ptr, nnz))
 
 
 def sort_mode(ctx: Context, idx_dev_ptr: int, dims: Sequence[int], nnz: int, mode: int, perm_dev_ptr: int):
