@@ -70,7 +70,10 @@ int ptg_ctx_synchronize(ptg_ctx *ctx);
 
 /* Context options (GB300 knobs, no reference counterpart). */
 typedef enum {
-  PTG_OPT_MTTKRP_IMPL = 1 /* 0: auto (tensor cores for BF16 storage), 1: CUDA cores, 2: tensor cores */
+  PTG_OPT_MTTKRP_IMPL = 1 /* 0: auto (tensor cores for BF16 storage), 1: CUDA cores,
+                             2: tensor cores (BF16: kind::f16; FP32, R <= 64: kind::tf32 with a
+                             three-term split, 2-3e-6 relative with a negative bias that grows
+                             with the contraction length) */
 } ptg_option;
 int ptg_ctx_set_option(ptg_ctx *ctx, int option, long long value);
 

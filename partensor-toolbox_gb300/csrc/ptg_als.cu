@@ -35,7 +35,6 @@ struct AlsBuffers {
   double *dsc = nullptr;  // [N][2]: <M, A>, sum(Z .* G); [N][2..3]: cost terms of a point
   int *isc = nullptr;     // [N][2]: iterations, repaired
   double *W = nullptr;    // R x R FP64: Z^{-1} or (M^T M)^{-1/2} (other constraints)
-  float *MtM = nullptr;   // R x R FP32 Gram of M (orthogonality)
   void *base = nullptr;
 
   int alloc(const int64_t *dims, int order, int rank, int64_t rows_left = 0, int64_t rows_right = 0) {
@@ -70,7 +69,6 @@ struct AlsBuffers {
     const size_t o_d = take(sizeof(double) * 4 * N);
     const size_t o_i = take(sizeof(int) * 2 * N);
     const size_t o_W = take(sizeof(double) * R * R);
-    const size_t o_C = take(sizeof(float) * R * R);
     cudaError_t e = cudaMalloc(&base, off);
     if (e != cudaSuccess) {
       base = nullptr;
@@ -92,7 +90,6 @@ struct AlsBuffers {
     dsc = (double *)(b + o_d);
     isc = (int *)(b + o_i);
     W = (double *)(b + o_W);
-    MtM = (float *)(b + o_C);
     return PTG_OK;
   }
   ~AlsBuffers() {
@@ -181,9 +178,7 @@ struct Runner {
       PTG_TRY(launch_update_unconstrained(ctx, b.M, b.fac[n], b.rows[n], R, b.np, b.W, S));
     } else if (con == PTG_ORTHOGONALITY) {
       if (b.rows[n] < R) return set_error(PTG_ERR_INVALID, "orthogonality needs I_n >= R");
-      PTG_TRY(launch_gram(b.M, b.rows[n], R, b.MtM, b.gpart, S));
-      count_launches(ctx, 2);
-      PTG_TRY(launch_update_orthogonal(ctx, b.M, b.fac[n], b.rows[n], R, b.MtM, b.W, S));
+      PTG_TRY(launch_update_orthogonal(ctx, b.M, b.fac[n], b.rows[n], R, b.W, S));
     } else if (con != PTG_SPARSITY && con != PTG_CONSTANT) {
       return set_error(PTG_ERR_INVALID, "unknown constraint");
     }

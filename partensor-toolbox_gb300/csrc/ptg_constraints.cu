@@ -1,6 +1,7 @@
 // Factor updates for the constraints other than nonnegativity (include/Cpd.hpp:189-228):
 //   unconstrained   A = M Z^{-1}                        (:196-199)
-//   orthogonality   A = M (M^T M)^{-1/2}, (M^T M)^{-1/2} = V diag(lambda^{-1/2}) V^T  (:210-217)
+//   orthogonality   A = M (M^T M)^{-1/2}, (M^T M)^{-1/2} = V diag(lambda^{-1/2}) V^T  (:210-217),
+//                   with M^T M accumulated in FP64
 //   sparsity, constant: the factor is kept (:219-222).
 // The R x R algebra runs in FP64 in one CTA (R <= 64): Gauss-Jordan elimination with partial
 // pivoting for Z^{-1} (the reference calls Eigen's inverse(), an LU with partial pivoting),
@@ -79,9 +80,23 @@ __global__ void __launch_bounds__(kAlgThreads) inverse_kernel(const NnlsParams *
   for (int idx = tid; idx < R * R; idx += blockDim.x) W[idx] = aug[(idx / R) * C + R + idx % R];
 }
 
-// W = (C)^{-1/2} for the symmetric positive definite C = M^T M (FP32 Gram, promoted to FP64),
-// through the cyclic Jacobi eigendecomposition C = V diag(lambda) V^T.
-__global__ void __launch_bounds__(kAlgThreads) inv_sqrt_kernel(const float *__restrict__ Cg, int R,
+constexpr int kGramRows = 256;
+
+// FP64 partial Grams of M (rows of one block each): part[b][i][j] = sum_rows M[r][i] M[r][j].
+__global__ void gram64_partial_kernel(const float *__restrict__ M, int I, int R, double *__restrict__ part) {
+  const int r0 = blockIdx.x * kGramRows;
+  const int nr = min(kGramRows, I - r0);
+  for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
+    const int a = idx / R, b = idx % R;
+    double s = 0.0;
+    for (int i = 0; i < nr; ++i) s = fma((double)M[(size_t)(r0 + i) * R + a], (double)M[(size_t)(r0 + i) * R + b], s);
+    part[(size_t)blockIdx.x * R * R + idx] = s;
+  }
+}
+
+// W = (C)^{-1/2} for the symmetric positive definite C = M^T M (the FP64 sum of the nb partial
+// Grams, in block order), through the cyclic Jacobi eigendecomposition C = V diag(lambda) V^T.
+__global__ void __launch_bounds__(kAlgThreads) inv_sqrt_kernel(const double *__restrict__ part, int nb, int R,
                                                                double *__restrict__ W, int *__restrict__ status) {
   extern __shared__ double sh[];
   const int n = R + (R & 1);   // even; an odd R gets an uncoupled padding index
@@ -94,7 +109,12 @@ __global__ void __launch_bounds__(kAlgThreads) inv_sqrt_kernel(const float *__re
   const int tid = threadIdx.x;
   for (int idx = tid; idx < n * n; idx += blockDim.x) {
     const int i = idx / n, j = idx % n;
-    A[idx] = (i < R && j < R) ? (double)Cg[i * R + j] : (i == j ? 1.0 : 0.0);
+    double c = i == j ? 1.0 : 0.0;
+    if (i < R && j < R) {
+      c = 0.0;
+      for (int b = 0; b < nb; ++b) c += part[(size_t)b * R * R + i * R + j];
+    }
+    A[idx] = c;
     V[idx] = i == j ? 1.0 : 0.0;
   }
   __syncthreads();
@@ -110,17 +130,17 @@ __global__ void __launch_bounds__(kAlgThreads) inv_sqrt_kernel(const float *__re
     __syncthreads();
     return s_off;
   };
-  double part = 0.0;
-  for (int idx = tid; idx < n * n; idx += blockDim.x) part += A[idx] * A[idx];
-  const double nrm2 = block_sum(part);
+  double sq = 0.0;
+  for (int idx = tid; idx < n * n; idx += blockDim.x) sq += A[idx] * A[idx];
+  const double nrm2 = block_sum(sq);
   if (tid == 0) s_nrm = nrm2;
   __syncthreads();
   const int half = n / 2;
   for (int sweep = 0; sweep < 40; ++sweep) {
-    part = 0.0;
+    sq = 0.0;
     for (int idx = tid; idx < n * n; idx += blockDim.x)
-      if (idx / n != idx % n) part += A[idx] * A[idx];
-    const double off = block_sum(part);
+      if (idx / n != idx % n) sq += A[idx] * A[idx];
+    const double off = block_sum(sq);
     if (off <= 1e-30 * s_nrm) break;
     for (int step = 0; step < n - 1; ++step) {
       // round-robin pairing: index 0 fixed, the others rotate
@@ -213,16 +233,19 @@ int launch_update_unconstrained(ptg_ctx *ctx, const float *M, float *A, int I, i
   return PTG_OK;
 }
 
-int launch_update_orthogonal(ptg_ctx *ctx, const float *M, float *A, int I, int R, const float *MtM, double *W,
-                             cudaStream_t s) {
+int launch_update_orthogonal(ptg_ctx *ctx, const float *M, float *A, int I, int R, double *W, cudaStream_t s) {
   if (R > kMaxR) return set_error(PTG_ERR_UNSUPPORTED, "rank > 64 is not supported by the orthogonal update");
+  const int nb = (I + kGramRows - 1) / kGramRows;
+  PTG_TRY(ctx->scratch.ensure(sizeof(double) * nb * R * R));   // MTTKRP partials are consumed by now
+  double *part = reinterpret_cast<double *>(ctx->scratch.ptr);
+  gram64_partial_kernel<<<nb, 256, 0, s>>>(M, I, R, part);
   const int n = R + (R & 1);
   const size_t smem = sizeof(double) * (2 * n * n + n) + sizeof(int) * n + 16;
   PTG_CUDA(cudaFuncSetAttribute(inv_sqrt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  inv_sqrt_kernel<<<1, kAlgThreads, smem, s>>>(MtM, R, W, ctx->dev_err);
+  inv_sqrt_kernel<<<1, kAlgThreads, smem, s>>>(part, nb, R, W, ctx->dev_err);
   rows_times_kernel<<<(I + 7) / 8, 256, 0, s>>>(M, W, I, R, A);
   PTG_CUDA(cudaGetLastError());
-  count_launches(ctx, 2);
+  count_launches(ctx, 3);
   return PTG_OK;
 }
 

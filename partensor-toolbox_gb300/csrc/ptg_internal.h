@@ -137,6 +137,9 @@ int launch_leaf_mttkrp(ptg_ctx *ctx, const ptg_tensor *t, const float *T, const 
 // tcgen05 (tensor-core) form of contraction_launch; BF16 storage only.
 int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                           cudaStream_t stream);
+// FP32 storage on the tensor cores (tcgen05 kind::tf32, three-term split), R <= 64.
+int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
+                            cudaStream_t stream);
 // Reads and clears the device error word (synchronises the stream first).
 int check_device_error(ptg_ctx *ctx);
 
@@ -203,11 +206,10 @@ int launch_accel_combine(const float *const *cur, const float *const *old, float
 // out2[0] = <M, A_last> (FP64), out2[1] = sum(Z_last .* G_last) with Z_last the Hadamard
 // of grams[0..order-2].
 // update_factor for unconstrained (A = M Z^{-1}, Z in np->Z) and orthogonal (A = M (M^T M)^{-1/2},
-// MtM the FP32 Gram of M) modes; W is an R x R FP64 scratch.  ptg_constraints.cu.
+// with the Gram of M in FP64) modes; W is an R x R FP64 scratch.  ptg_constraints.cu.
 int launch_update_unconstrained(ptg_ctx *ctx, const float *M, float *A, int I, int R, const NnlsParams *np,
                                 double *W, cudaStream_t s);
-int launch_update_orthogonal(ptg_ctx *ctx, const float *M, float *A, int I, int R, const float *MtM, double *W,
-                             cudaStream_t s);
+int launch_update_orthogonal(ptg_ctx *ctx, const float *M, float *A, int I, int R, double *W, cudaStream_t s);
 int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const float *const *grams,
                       int order, int R, double *out2, cudaStream_t stream);
 

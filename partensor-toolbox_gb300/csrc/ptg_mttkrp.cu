@@ -739,8 +739,13 @@ int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, 
   cudaEvent_t ev = nullptr;
   PTG_TRY(stats_begin(ctx, stream, &ev));
   int rc;
-  const bool tc = t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 128;
-  if (t->dtype == PTG_F32)
+  // FP32 storage reaches the tensor cores (three-term TF32 split) only on request: its
+  // accumulation in TMEM carries a small negative bias that grows with the contraction length
+  const bool tc = (t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 128) ||
+                  (t->dtype == PTG_F32 && R <= 64 && ctx->mttkrp_impl == 2);
+  if (t->dtype == PTG_F32 && tc)
+    rc = tc32_contraction_launch(ctx, t, c, R, out, stream);
+  else if (t->dtype == PTG_F32)
     rc = launch_typed<float>(ctx, t, c, R, out, stream);
   else if (tc)
     rc = tc_contraction_launch(ctx, t, c, R, out, stream);

@@ -18,9 +18,12 @@
 #include <mutex>
 
 #include "ptg_internal.h"
+#include "ptg_tcgen05.h"
 
 namespace ptg {
 namespace {
+
+using namespace tc;
 
 constexpr int TC_BM = 128;         // q rows per tile (MMA M)
 constexpr int TC_BK = 64;          // contraction elements per K-block (one 128-byte row)
@@ -28,14 +31,6 @@ constexpr int TC_STAGES = 8;       // X tile ring
 constexpr int TC_KSTAGES = 4;      // Khatri-Rao tile ring
 constexpr int TC_THREADS = 192;
 constexpr int TC_ATILE = TC_BM * TC_BK * 2;   // 16 KB
-constexpr uint32_t kSpinLimit = 1u << 26;
-
-struct KrDevTc {
-  int n;
-  uint32_t ext[PTG_MAX_ORDER];
-  uint32_t valid[PTG_MAX_ORDER];
-  const float *fac[PTG_MAX_ORDER];
-};
 
 struct TcParams {
   int64_t P, Q, S;
@@ -49,118 +44,6 @@ struct TcParams {
   float *partial;  // [nsplit][Q][N]
   int *err;
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait; false when it gave up (or another role already gave up).
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 1023) == 1023 && *abort) return false;
-  }
-  return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1,
-                                            int c2) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
-      : "memory");
-}
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
-      ::"r"(smem_u32(dst)), "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void fence_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-// Shared-memory matrix descriptor (tcgen05): start, leading/stride byte offsets, fixed
-// version bits 46-48 = 0b001, 128-byte swizzle (layout type 2 in bits 61-63).
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
-  return d;
-}
-
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
-      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void umma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-// Khatri-Rao values of one side for linear index `lin`, 8 consecutive columns from c.
-__device__ __forceinline__ void kr8(const KrDevTc &s, uint32_t lin, int R, int c, float *v) {
-#pragma unroll
-  for (int j = 0; j < 8; ++j) v[j] = 1.0f;
-  for (int f = 0; f < s.n; ++f) {
-    const uint32_t e = s.ext[f];
-    const uint32_t d = lin % e;
-    lin /= e;
-    if (d >= s.valid[f]) {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) v[j] = 0.0f;
-      return;
-    }
-    const float *row = s.fac[f] + (size_t)d * R;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) v[j] *= (c + j < R) ? __ldg(row + c + j) : 0.0f;
-  }
-}
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
 mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
@@ -394,26 +277,6 @@ __global__ void tc_reduce_kernel(const float *__restrict__ partial, int nsplit, 
     for (int sp = 0; sp < nsplit; ++sp) s += partial[((int64_t)sp * Q + q) * N + c];
     out[idx] = s;
   }
-}
-
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-    cudaGetLastError();
-  });
-  return fn;
 }
 
 size_t tc_smem_bytes(int N) {
