@@ -226,6 +226,27 @@ int ptg_cpd_dimtree(ptg_ctx *ctx, int order, const int64_t *dims, const double *
                     const double *const *init_factors, double *const *out_factors,
                     ptg_cpd_result *result, ptg_sweep_trace *trace);
 
+/* ---- File-based entry points ---------------------------------------------------------
+ * The reference's raw files (include/ReadWrite.hpp:100-130, 293-345): a tensor file holds
+ * prod(dims) FP64 values in ColMajor order after `skip` values; a factor file holds an I x R
+ * FP64 matrix in row-major order (the reference writes the transpose of the ColMajor
+ * MatrixXd).  The tensor is streamed through page-locked memory into HBM and converted there.
+ * ptg_tensor_create_file replaces read(path, size, skip, tnsX) + the upload;
+ * ptg_cpd_file / ptg_cpd_dimtree_file replace cpd(tnsDims, R, path[, options]) and
+ * cpd(tnsDims, R, paths[, options]) (include/Cpd.hpp:591-850) and the cpdDimTree overloads:
+ * factor_paths = NULL draws the initial factors U[0,1] from `seed` (the reference's
+ * makeFactors draws them from the clock). */
+int ptg_tensor_create_file(ptg_ctx *ctx, int order, const int64_t *dims, ptg_dtype dtype, const char *path,
+                           int64_t skip, ptg_tensor **out);
+int ptg_cpd_file(ptg_ctx *ctx, int order, const int64_t *dims, const char *tensor_path, int64_t skip,
+                 const char *const *factor_paths, unsigned long long seed, ptg_dtype dtype, int rank,
+                 const ptg_cpd_options *opts, double *const *out_factors, ptg_cpd_result *result,
+                 ptg_sweep_trace *trace);
+int ptg_cpd_dimtree_file(ptg_ctx *ctx, int order, const int64_t *dims, const char *tensor_path, int64_t skip,
+                         const char *const *factor_paths, unsigned long long seed, ptg_dtype dtype, int rank,
+                         const ptg_cpd_options *opts, double *const *out_factors, ptg_cpd_result *result,
+                         ptg_sweep_trace *trace);
+
 /* ---- Many small CPDs in one call ------------------------------------------------------
  * Solves n independent nonnegative CPD-ALS problems of the same order (ranks and dims may
  * differ per instance) with the semantics of ptg_cpd on an FP32 tensor, each instance

@@ -39,10 +39,16 @@ class SparseOptions:
     c_stochastic_perc: float = 0.5
     lambdas: Optional[List[float]] = None
     seed: int = 0
+    constraints: Optional[List[int]] = None   # Constraint values (include/Constants.hpp:49-57)
 
     def __post_init__(self):
         if self.lambdas is None:
             self.lambdas = [0.01] * self.order
+        if self.constraints is None:
+            self.constraints = [NONNEGATIVITY] * self.order
+
+
+UNCONSTRAINED, NONNEGATIVITY = 0, 1
 
 
 @dataclasses.dataclass
@@ -165,6 +171,14 @@ def local_L_nesterov(factors: List[np.ndarray], mm: ModeMatrix, M: np.ndarray, m
     return A
 
 
+def ridge_update(factors: List[np.ndarray], mm: ModeMatrix, M: np.ndarray, lam: float) -> np.ndarray:
+    """unconstraint_update (include/Gtc.hpp:275-315): row i = (H_i + lambda I)^{-1} m_i with
+    H_i = sum kr kr^T and m_i = sum x kr over the row's entries."""
+    H = row_hessians(factors, mm)
+    R = H.shape[1]
+    return np.stack([np.linalg.solve(H[i] + lam * np.eye(R), M[i]) for i in range(H.shape[0])])
+
+
 def gtc_cost(factors: Sequence[np.ndarray], idx: np.ndarray, vals: np.ndarray) -> float:
     """sum over observed entries of (x - sum_r prod_k A_k(i_k, r))^2, include/Gtc.hpp:184-214."""
     pred = np.ones((idx.shape[1], factors[0].shape[1]))
@@ -196,9 +210,17 @@ def gtc(idx: np.ndarray, vals: np.ndarray, dims: Sequence[int], R: int, options:
     while True:
         st.ao_iter += 1
         for n in range(N):
+            # update_factor's switch (include/Gtc.hpp:330-355): unconstrained -> ridge solve,
+            # nonnegativity -> local_L Nesterov, every other constraint keeps the factor
+            con = options.constraints[n]
+            if con not in (UNCONSTRAINED, NONNEGATIVITY):
+                continue
             M = sparse_mttkrp(st.factors, mms[n])
-            st.factors[n] = local_L_nesterov(st.factors, mms[n], M, options.max_nesterov_iter,
-                                             options.lambdas[n])
+            if con == UNCONSTRAINED:
+                st.factors[n] = ridge_update(st.factors, mms[n], M, options.lambdas[n])
+            else:
+                st.factors[n] = local_L_nesterov(st.factors, mms[n], M, options.max_nesterov_iter,
+                                                 options.lambdas[n])
         st.f_value = gtc_cost(st.factors, idx, vals)
         st.rel_costFunction = st.f_value / st.frob_tns
         st.trace.append(dict(f_value=st.f_value, rel=st.rel_costFunction))
@@ -274,6 +296,10 @@ def gtc_stochastic(idx: np.ndarray, vals: np.ndarray, dims: Sequence[int], R: in
     while True:
         st.ao_iter += 1
         for n in range(N):
+            # the stochastic update_factor (include/GtcStochastic.hpp:325-345) updates only the
+            # nonnegative modes; every other constraint, unconstrained included, keeps the factor
+            if options.constraints[n] != NONNEGATIVITY:
+                continue
             st.factors[n] = stochastic_nesterov(st.factors, mms[n], options.c_stochastic_perc,
                                                 options.max_nesterov_iter, options.lambdas[n],
                                                 options.seed, st.ao_iter)

@@ -9,8 +9,8 @@ raises.
 """
 from . import _lib  # noqa: F401
 from .cpd import (CONSTANT, NONNEGATIVITY, ORTHOGONALITY, SPARSITY, UNCONSTRAINED, Context,  # noqa: F401
-                  Options, Status, Tensor, WarmStartModel, cpd, cpd_batched, cpd_resident, cpdDimTree, default_context,
-                  mttkrp)
+                  Options, Status, Tensor, WarmStartModel, cpd, cpd_batched, cpd_file, cpd_resident, cpdDimTree,
+                  default_context, mttkrp, write_factor_file, write_tensor_file)
 from .gtc import SparseOptions, SparseStatus, gtc, gtc_coo, gtc_device, gtc_stochastic  # noqa: F401
 from .gtc import sort_mode as gtc_sort_mode  # noqa: F401
 from ._lib import PtgError  # noqa: F401

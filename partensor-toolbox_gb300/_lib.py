@@ -23,6 +23,7 @@ EXPORTS = [
     "ptg_tensor_create", "ptg_tensor_destroy", "ptg_tensor_norms",
     "ptg_mttkrp", "ptg_cpd_default_options", "ptg_cpd_als", "ptg_cpd",
     "ptg_cpd_dimtree_als", "ptg_cpd_dimtree", "ptg_mttkrp_noalloc", "ptg_cpd_batched",
+    "ptg_tensor_create_file", "ptg_cpd_file", "ptg_cpd_dimtree_file",
     "ptg_gtc_default_options", "ptg_gtc", "ptg_gtc_sort_mode",
     "ptg_mlp_create", "ptg_mlp_destroy", "ptg_mlp_num_params", "ptg_mlp_get_params", "ptg_mlp_set_params",
     "ptg_mlp_forward", "ptg_mlp_loss_grad", "ptg_mlp_train",
@@ -141,6 +142,13 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ptg_mlp_train.argtypes = [vp, vp, vp, vp, ctypes.c_longlong, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                   ctypes.c_ulonglong, dp]
     lib.ptg_cpd_dimtree_als.argtypes = lib.ptg_cpd_als.argtypes
+    cpp = ctypes.POINTER(ctypes.c_char_p)
+    lib.ptg_tensor_create_file.argtypes = [vp, ctypes.c_int, i64p, ctypes.c_int, ctypes.c_char_p, ctypes.c_int64,
+                                           ctypes.POINTER(vp)]
+    lib.ptg_cpd_file.argtypes = [vp, ctypes.c_int, i64p, ctypes.c_char_p, ctypes.c_int64, cpp, ctypes.c_ulonglong,
+                                 ctypes.c_int, ctypes.c_int, ctypes.POINTER(CpdOptions), dpp,
+                                 ctypes.POINTER(CpdResult), ctypes.POINTER(SweepTrace)]
+    lib.ptg_cpd_dimtree_file.argtypes = lib.ptg_cpd_file.argtypes
     lib.ptg_cpd_batched.argtypes = [vp, ctypes.c_int, ctypes.POINTER(CpdInstance), ctypes.POINTER(CpdOptions),
                                     ctypes.POINTER(CpdResult), dp]
     lib.ptg_cpd_dimtree.argtypes = lib.ptg_cpd.argtypes

@@ -368,3 +368,46 @@ def cpd_batched(problems: Sequence[tuple], options: Optional[Options] = None,
     check(ctx._lib.ptg_cpd_batched(ctx.handle, n, insts, ctypes.byref(options.to_c()), res,
                                    secs.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
     return [_status_from(options, outs_all[i], res[i], None, 0) for i in range(n)], secs
+
+
+def cpd_file(tnsDims: Sequence[int], R: int, path, options: Optional[Options] = None, skip: int = 0,
+             seed: int = 0, ctx: Optional[Context] = None, dimtree: bool = False) -> Status:
+    """partensor::cpd(tnsDims, R, path[, options]) and cpd(tnsDims, R, paths[, options])
+    (include/Cpd.hpp:591-850): ``path`` is the tensor file (prod(dims) FP64 values, ColMajor,
+    after ``skip`` values), or a sequence [tensor path, factor paths...] whose factor files
+    hold I_k x R FP64 row-major matrices (the format of include/ReadWrite.hpp).  Without
+    factor files the initial factors are U[0,1] from ``seed`` (``ptg_cpd_file``)."""
+    ctx = ctx or default_context()
+    dims = [int(d) for d in tnsDims]
+    N = len(dims)
+    options = options or Options(order=N)
+    if isinstance(path, (str, bytes)):
+        tpath, fpaths = path, None
+    else:
+        tpath, fpaths = path[0], list(path[1:])
+        if len(fpaths) != N:
+            raise ValueError("paths must hold the tensor path and one factor path per mode")
+    enc = lambda p: p.encode() if isinstance(p, str) else p
+    fp = None
+    if fpaths is not None:
+        fp = (ctypes.c_char_p * N)(*[enc(p) for p in fpaths])
+    outs = [np.zeros((dims[k], R), order="F") for k in range(N)]
+    op = (ctypes.POINTER(ctypes.c_double) * N)(*[_dptr(x) for x in outs])
+    d = (ctypes.c_int64 * N)(*dims)
+    res = CpdResult()
+    ntr = options.max_iter + max(0, options.refine_sweeps)
+    trace = (SweepTrace * ntr)()
+    fn = ctx._lib.ptg_cpd_dimtree_file if dimtree else ctx._lib.ptg_cpd_file
+    check(fn(ctx.handle, N, d, enc(tpath), int(skip), fp, int(seed), DTYPES[options.precision], int(R),
+             ctypes.byref(options.to_c()), op, ctypes.byref(res), trace))
+    return _status_from(options, outs, res, trace, res.ao_iter + res.refine_sweeps_done)
+
+
+def write_tensor_file(path, X: np.ndarray):
+    """Writes X in the reference's tensor file format (FP64, ColMajor)."""
+    np.asfortranarray(np.asarray(X, dtype=np.float64)).reshape(-1, order="F").tofile(path)
+
+
+def write_factor_file(path, A: np.ndarray):
+    """Writes an I x R factor in the reference's factor file format (FP64, row-major)."""
+    np.ascontiguousarray(np.asarray(A, dtype=np.float64)).tofile(path)

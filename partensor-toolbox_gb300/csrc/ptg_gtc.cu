@@ -274,6 +274,8 @@ struct RowArgs {
   int outer;
   // cost
   double *row_cost;        // optional: per-row sum of squared residuals with the new row
+  int ridge;               // 1: unconstraint_update, a_i = (H_i + lambda I)^{-1} m_i
+  int *err;                // device error word (a non-positive pivot in the ridge solve)
 };
 
 // Hadamard of the other modes' factor rows for entry s, multiplied from the last mode down
@@ -423,6 +425,46 @@ __device__ float power_method_warp(RowShared &sh, int R, float eps) {
   return lam;
 }
 
+// unconstraint_update (include/Gtc.hpp:275-315) by warp 0: sh.a = (H + lambda I)^{-1} m through
+// a Cholesky factorisation in place in the lower triangle of sh.H (FP32; lambda > 0 keeps the
+// system positive definite), then the two triangular solves.
+__device__ void ridge_solve_warp(RowShared &sh, int R, float lam, int *err) {
+  const int lane = threadIdx.x & 31;
+  bool bad = false;
+  for (int j = 0; j < R; ++j) {
+    float s = 0.0f;
+    for (int k = lane; k < j; k += 32) s = fmaf(sh.H[j][k], sh.H[j][k], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const float d2 = sh.H[j][j] + lam - s;
+    bad |= !(d2 > 0.0f);
+    const float d = sqrtf(fmaxf(d2, 1e-30f));
+    __syncwarp();
+    for (int i = j + 1 + lane; i < R; i += 32) {
+      float t = sh.H[i][j];
+      for (int k = 0; k < j; ++k) t = fmaf(-sh.H[i][k], sh.H[j][k], t);
+      sh.H[i][j] = t / d;
+    }
+    if (lane == 0) sh.H[j][j] = d;
+    __syncwarp();
+  }
+  // L y = m (y in sh.y), then L^T a = y
+  for (int i = 0; i < R; ++i) {
+    float s = 0.0f;
+    for (int k = lane; k < i; k += 32) s = fmaf(sh.H[i][k], sh.y[k], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sh.y[i] = (sh.m[i] - s) / sh.H[i][i];
+    __syncwarp();
+  }
+  for (int i = R - 1; i >= 0; --i) {
+    float s = 0.0f;
+    for (int k = i + 1 + lane; k < R; k += 32) s = fmaf(sh.H[k][i], sh.a[k], s);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sh.a[i] = (sh.y[i] - s) / sh.H[i][i];
+    __syncwarp();
+  }
+  if (bad && lane == 0) atomicExch(err, PTG_ERR_NUMERIC);
+}
+
 // One projected Nesterov step of warp 0: grad = H y - m + lambda * (y + prox * a_prev)
 __device__ void nesterov_step_warp(RowShared &sh, int R, float lam, float invL, float beta, float prox) {
   const int lane = threadIdx.x & 31;
@@ -473,7 +515,9 @@ __global__ void __launch_bounds__(GT_THREADS) gtc_row_kernel(const RowArgs a) {
     }
     tiles_store(sh, R, acc, macc);
     __syncthreads();
-    if (tid < 32 && cnt_row > 0) {
+    if (a.ridge) {
+      if (tid < 32) ridge_solve_warp(sh, R, a.lambda, a.err);   // an empty row gives a_i = 0
+    } else if (tid < 32 && cnt_row > 0) {
       const float L = power_method_warp(sh, R, 1e-3f) + a.lambda;
       const float invL = 1.0f / L;
       const float sq = sqrtf(a.lambda * invL);
@@ -728,8 +772,8 @@ int ptg_gtc(ptg_ctx *ctx, int order, const int64_t *dims, int64_t nnz, const int
   if (opt->max_iter < 1 || opt->max_nesterov_iter < 0) return set_error(PTG_ERR_INVALID, "bad iteration limits");
   for (int k = 0; k < order; ++k) {
     if (dims[k] < 1 || dims[k] > 0x7fffffffLL) return set_error(PTG_ERR_INVALID, "bad dimension");
-    if (opt->constraints[k] != PTG_NONNEGATIVITY)
-      return set_error(PTG_ERR_UNSUPPORTED, "GTC: only nonnegativity constraints are implemented");
+    if (opt->constraints[k] < PTG_UNCONSTRAINED || opt->constraints[k] > PTG_CONSTANT)
+      return set_error(PTG_ERR_UNSUPPORTED, "GTC: symmetric constraints are not implemented");
   }
   PTG_CUDA(cudaSetDevice(ctx->device));
   const auto t0 = std::chrono::steady_clock::now();
@@ -833,6 +877,8 @@ int ptg_gtc(ptg_ctx *ctx, int order, const int64_t *dims, int64_t nnz, const int
     a.stochastic = opt->stochastic;
     a.c = (float)opt->c_stochastic_perc;
     a.seed = opt->seed;
+    a.ridge = 0;
+    a.err = ctx->dev_err;
     return a;
   };
   auto cost = [&](double *f) -> int {
@@ -865,8 +911,15 @@ int ptg_gtc(ptg_ctx *ctx, int order, const int64_t *dims, int64_t nnz, const int
   for (;;) {
     ++ao_iter;
     for (int n = 0; n < N; ++n) {
+      // update_factor (include/Gtc.hpp:330-355; include/GtcStochastic.hpp:325-345): the full
+      // form updates unconstrained modes by the ridge solve and nonnegative modes by local_L
+      // Nesterov, the stochastic form only the nonnegative modes; every other mode is kept
+      const int con = opt->constraints[n];
+      const bool ridge = !opt->stochastic && con == PTG_UNCONSTRAINED;
+      if (!ridge && con != PTG_NONNEGATIVITY) continue;
       RowArgs a = make_args(n);
       a.outer = ao_iter;
+      a.ridge = ridge ? 1 : 0;
       gtc_row_kernel<<<(unsigned)dims[n], GT_THREADS, smem, S>>>(a);
       count_launches(ctx, 1);
       PTG_CUDA(cudaGetLastError());

@@ -32,10 +32,13 @@ class SparseOptions:
     lambdas: Optional[List[float]] = None
     seed: int = 0
     factorsInit: Optional[List[np.ndarray]] = None
+    constraints: Optional[List[int]] = None   # default nonnegativity on every mode
 
     def __post_init__(self):
         if self.lambdas is None:
             self.lambdas = [0.01] * self.order
+        if self.constraints is None:
+            self.constraints = [1] * self.order
 
 
 @dataclasses.dataclass
@@ -75,6 +78,7 @@ def _run(idx, vals, options: SparseOptions, stochastic: bool, ctx: Optional[Cont
     o.c_stochastic_perc = options.c_stochastic_perc
     for k in range(N):
         o.lambdas[k] = options.lambdas[k]
+        o.constraints[k] = int(options.constraints[k])
     o.stochastic = int(stochastic)
     o.seed = options.seed
     if options.factorsInit is None:

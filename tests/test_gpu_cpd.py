@@ -192,3 +192,29 @@ def test_orthogonal_factor_is_orthonormal(pkg, ctx):
                                    acceleration=False), init, ctx=ctx)
     Q = st.factors[0]
     assert np.abs(Q.T @ Q - np.eye(4)).max() < 1e-4
+
+
+def test_cpd_from_files_matches_in_memory(pkg, ctx, tmp_path):
+    """cpd(tnsDims, R, paths[, options]) with the reference's file formats (ColMajor FP64
+    tensor after `skip` values, row-major FP64 factors): the same result as the in-memory call."""
+    X, _, init = _cfg1_like((30, 26, 22), 4, seed=31)
+    tpath = tmp_path / "x.bin"
+    # 5 leading values to skip, as read(path, size, skip, ...) allows
+    np.concatenate([np.full(5, 7.0), np.asfortranarray(X).reshape(-1, order="F")]).tofile(tpath)
+    fpaths = []
+    for k, A in enumerate(init):
+        fpaths.append(str(tmp_path / f"a{k}.bin"))
+        pkg.write_factor_file(fpaths[-1], A)
+    o = pkg.Options(order=3, max_iter=6)
+    st_f = pkg.cpd_file(X.shape, 4, [str(tpath)] + fpaths, o, skip=5, ctx=ctx)
+    st_m = pkg.cpd(X, 4, o, init, ctx=ctx)
+    for k in range(3):
+        assert np.array_equal(st_f.factors[k], st_m.factors[k])
+    assert st_f.f_value == st_m.f_value
+    # the tensor alone, with seeded initial factors: a valid run, reproducible
+    pkg.write_tensor_file(tmp_path / "y.bin", X)
+    a = pkg.cpd_file(X.shape, 4, str(tmp_path / "y.bin"), o, seed=3, ctx=ctx)
+    b = pkg.cpd_file(X.shape, 4, str(tmp_path / "y.bin"), o, seed=3, ctx=ctx)
+    assert np.array_equal(a.factors[0], b.factors[0]) and np.isfinite(a.f_value)
+    with pytest.raises(pkg.PtgError):
+        pkg.cpd_file((31, 26, 22), 4, str(tmp_path / "y.bin"), o, ctx=ctx)   # file too short

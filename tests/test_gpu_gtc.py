@@ -86,3 +86,34 @@ def test_gtc_rejects_duplicates(pkg, ctx):
     with pytest.raises(pkg._lib.PtgError) as e:
         pkg.gtc_coo(idx, vals, o, ctx=ctx)
     assert e.value.code == pkg._lib.PTG_ERR_INVALID
+
+
+@pytest.mark.parametrize("cons", [(0, 0, 0), (1, 0, 1), (0, 4, 1)])
+def test_gtc_constraints_match_oracle(pkg, ctx, cons):
+    """update_factor of include/Gtc.hpp:330-355: unconstrained modes by the ridge solve
+    (H_i + lambda I)^{-1} m_i (FP32 Cholesky here, FP64 inverse in the oracle), nonnegative modes
+    by local_L Nesterov, a constant mode kept."""
+    dims, R = (40, 36, 30), 4
+    idx, vals, init = _problem(dims, 12000, R, 11)
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=5, lambdas=[1e-2] * 3,
+                          factorsInit=init, constraints=list(cons))
+    st = pkg.gtc_coo(idx, vals, o, ctx=ctx)
+    ref = og.gtc(idx, vals, dims, R, og.SparseOptions(order=3, max_iter=5, lambdas=[1e-2] * 3,
+                                                      constraints=list(cons)), init)
+    rel_gpu = np.array([t["rel"] for t in st.trace])
+    rel_ref = np.array([t["rel"] for t in ref.trace])
+    assert np.max(np.abs(rel_gpu - rel_ref)) < 2e-4 * max(1.0, rel_ref.max()), (rel_gpu, rel_ref)
+    for k in range(3):
+        if cons[k] == 4:
+            assert np.allclose(st.factors[k], init[k], atol=1e-7)
+
+
+def test_gtc_stochastic_keeps_unconstrained_modes(pkg, ctx):
+    """The stochastic form updates only the nonnegative modes (include/GtcStochastic.hpp:325-345)."""
+    dims, R = (30, 28, 26), 3
+    idx, vals, init = _problem(dims, 8000, R, 13)
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=1, c_stochastic_perc=0.2,
+                          lambdas=[1e-3] * 3, factorsInit=init, constraints=[1, 0, 1])
+    st = pkg.gtc_coo(idx, vals, o, stochastic=True, ctx=ctx)
+    assert np.allclose(st.factors[1], init[1], atol=1e-7)
+    assert not np.allclose(st.factors[0], init[0], atol=1e-3)
