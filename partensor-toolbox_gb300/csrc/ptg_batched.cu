@@ -30,7 +30,7 @@
 namespace ptg {
 namespace {
 
-constexpr int BN_THREADS = 256;
+constexpr int BN_THREADS = 512;
 constexpr int BN_MAXR = 32;
 
 struct BNnls {
@@ -322,6 +322,19 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   PTG_CUDA(cudaStreamCreateWithFlags(&sh.s, cudaStreamNonBlocking));
   PTG_CUDA(cudaStreamSynchronize(ctx->stream));
   cudaStream_t S = sh.s;
+  // a second private stream: the eigenvalue bounds of a mode run beside its MTTKRP
+  struct SideHolder {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ~SideHolder() {
+      if (fork) cudaEventDestroy(fork);
+      if (join) cudaEventDestroy(join);
+      if (s) cudaStreamDestroy(s);
+    }
+  } side;
+  PTG_CUDA(cudaStreamCreateWithFlags(&side.s, cudaStreamNonBlocking));
+  PTG_CUDA(cudaEventCreateWithFlags(&side.fork, cudaEventDisableTiming));
+  PTG_CUDA(cudaEventCreateWithFlags(&side.join, cudaEventDisableTiming));
 
   // ---- one device block for every tensor and per-instance buffer ----
   std::vector<InstDesc> desc(n_inst);
@@ -701,8 +714,23 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   PTG_CUDA(cudaStreamBeginCapture(S, cudaStreamCaptureModeThreadLocal));
   int cap_rc = PTG_OK;
   for (int n = 0; n < N && cap_rc == PTG_OK; ++n) {
-    cap_rc = launch_eigen_batched(ctx, d_eig + (size_t)n * n_inst, n_inst, d_active, S);
+    // fork: eigenvalue bounds on the side stream, MTTKRP on the main one; join before the NNLS
+    cudaError_t fe = cudaEventRecord(side.fork, S);
+    if (fe == cudaSuccess) fe = cudaStreamWaitEvent(side.s, side.fork, 0);
+    if (fe != cudaSuccess) {
+      cap_rc = cuda_error(fe, "graph fork", __FILE__, __LINE__);
+      break;
+    }
+    cap_rc = launch_eigen_batched(ctx, d_eig + (size_t)n * n_inst, n_inst, d_active, side.s);
+    if (cap_rc == PTG_OK) {
+      fe = cudaEventRecord(side.join, side.s);
+      if (fe != cudaSuccess) cap_rc = cuda_error(fe, "graph join", __FILE__, __LINE__);
+    }
     if (cap_rc == PTG_OK) cap_rc = mttkrp_all(n, d_active);
+    if (cap_rc == PTG_OK) {
+      fe = cudaStreamWaitEvent(S, side.join, 0);
+      if (fe != cudaSuccess) cap_rc = cuda_error(fe, "graph join", __FILE__, __LINE__);
+    }
     if (cap_rc == PTG_OK) {
       nnls_block_kernel<<<n_inst, BN_THREADS, nnls_smem, S>>>(d_nn + (size_t)n * n_inst, d_active);
       count_launches(ctx, 1);

@@ -218,3 +218,29 @@ def test_cpd_from_files_matches_in_memory(pkg, ctx, tmp_path):
     assert np.array_equal(a.factors[0], b.factors[0]) and np.isfinite(a.f_value)
     with pytest.raises(pkg.PtgError):
         pkg.cpd_file((31, 26, 22), 4, str(tmp_path / "y.bin"), o, ctx=ctx)   # file too short
+
+
+def _nway_problem(dims, R, seed):
+    rng = np.random.default_rng(seed)
+    A = [rng.random((I, R)) for I in dims]
+    sub = "abcdefgh"[:len(dims)]
+    X = np.einsum(",".join(c + "r" for c in sub) + "->" + sub, *A)
+    X = X + 0.02 * X.std() * rng.standard_normal(dims)
+    init = [rng.random((I, R)) for I in dims]
+    return X, init
+
+
+@pytest.mark.parametrize("dims", [(9, 8, 7, 6, 5), (6, 5, 5, 4, 4, 3), (4, 4, 3, 3, 3, 3, 2), (3, 3, 3, 3, 2, 2, 2, 2)])
+def test_cpd_orders_5_to_8_match_oracle(pkg, ctx, dims):
+    """Orders 5-8 (the reference supports 3-8): cpd and cpdDimTree (split at (1+N)/2) follow
+    the FP64 oracle per sweep."""
+    N, R = len(dims), 3
+    X, init = _nway_problem(dims, R, 40 + N)
+    o = pkg.Options(order=N, max_iter=6)
+    ref = oc.cpd_als(X, R, oc.Options(order=N, max_iter=6), init)
+    rel_ref = np.array([s["rel"] for s in ref.trace])
+    for fn in (pkg.cpd, pkg.cpdDimTree):
+        st = fn(X, R, o, init, ctx=ctx)
+        rel = np.array([t["rel"] for t in st.trace])
+        assert st.ao_iter == ref.ao_iter
+        assert np.max(np.abs(rel - rel_ref)) < 1e-4, (fn.__name__, rel, rel_ref)
