@@ -73,7 +73,9 @@ typedef enum {
   PTG_OPT_MTTKRP_IMPL = 1 /* 0: auto (tensor cores for BF16 storage), 1: CUDA cores,
                              2: tensor cores (BF16: kind::f16; FP32, R <= 64: kind::tf32 with a
                              three-term split, 2-3e-6 relative with a negative bias that grows
-                             with the contraction length) */
+                             with the contraction length) */,
+  PTG_OPT_NNLS_CLUSTER = 2 /* CTAs of the NNLS thread-block cluster: 0 auto (16 where the device
+                             schedules it, else 8), or 2, 4, 8, 16 */
 } ptg_option;
 int ptg_ctx_set_option(ptg_ctx *ctx, int option, long long value);
 

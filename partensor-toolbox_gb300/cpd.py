@@ -105,6 +105,10 @@ class Context:
         """"auto" (tensor cores for BF16 storage), "cuda_cores" or "tensor_cores"."""
         check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_MTTKRP_IMPL, _lib.MTTKRP_IMPLS[impl]))
 
+    def set_nnls_cluster(self, size: int):
+        """CTAs of the NNLS cluster: 0 (auto), 2, 4, 8 or 16."""
+        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_NNLS_CLUSTER, int(size)))
+
     def enable_stats(self, on: bool = True):
         check(self._lib.ptg_ctx_enable_stats(self.handle, int(on)))
 

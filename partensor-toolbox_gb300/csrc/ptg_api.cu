@@ -260,6 +260,11 @@ int ptg_ctx_set_option(ptg_ctx *c, int option, long long value) {
       if (value < 0 || value > 2) return set_error(PTG_ERR_INVALID, "MTTKRP impl must be 0, 1 or 2");
       c->mttkrp_impl = (int)value;
       return PTG_OK;
+    case PTG_OPT_NNLS_CLUSTER:
+      if (value != 0 && value != 2 && value != 4 && value != 8 && value != 16)
+        return set_error(PTG_ERR_INVALID, "NNLS cluster size must be 0 (auto), 2, 4, 8 or 16");
+      c->nnls_cluster = (int)value;   // 0: probe again on the next solve
+      return PTG_OK;
     default:
       return set_error(PTG_ERR_INVALID, "unknown option");
   }
