@@ -232,6 +232,9 @@ int ptg_ctx_destroy(ptg_ctx *c) {
   for (cudaEvent_t e : c->stats.pool) cudaEventDestroy(e);
   if (c->dev_err) cudaFree(c->dev_err);
   if (c->pinned) cudaFreeHost(c->pinned);
+  c->stage64.release();
+  c->cache_x.release();
+  c->cache_xr.release();
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
   if (c->side) cudaStreamDestroy(c->side);
@@ -313,6 +316,15 @@ int ptg_ctx_reset_stats(ptg_ctx *c) {
 
 int ptg_tensor_create(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtype,
                       const double *src, int src_on_device, ptg_tensor **out) {
+  return ptg::tensor_create_impl(c, order, dims, dtype, src, src_on_device, nullptr, out);
+}
+
+}  // extern "C"
+
+namespace ptg {
+
+int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtype, const double *src,
+                       int src_on_device, DevBuf *storage, ptg_tensor **out) {
   if (!c || !dims || !src || !out) return set_error(PTG_ERR_INVALID, "NULL argument");
   *out = nullptr;
   if (order < 2 || order > PTG_MAX_ORDER)
@@ -333,8 +345,16 @@ int ptg_tensor_create(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtyp
   t->dtype = dtype;
   t->device = c->device;
   const size_t esz = dtype == PTG_F32 ? 4 : 2;
-  cudaError_t e = cudaMalloc(&t->data, (size_t)t->numel_padded * esz);
-  if (e != cudaSuccess) {
+  cudaError_t e = cudaSuccess;
+  if (storage) {   // a context-owned buffer, kept for the next call
+    const int rs = storage->ensure((size_t)t->numel_padded * esz);
+    if (rs != PTG_OK) {
+      delete t;
+      return rs;
+    }
+    t->data = storage->ptr;
+    t->owns = false;
+  } else if ((e = cudaMalloc(&t->data, (size_t)t->numel_padded * esz)) != cudaSuccess) {
     delete t;
     return cuda_error(e, "cudaMalloc(tensor)", __FILE__, __LINE__);
   }
@@ -427,7 +447,7 @@ int ptg_tensor_create(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtyp
   if (part) cudaFree(part);
   if (acc) cudaFree(acc);
   if (rc != PTG_OK) {
-    cudaFree(t->data);
+    if (t->owns) cudaFree(t->data);
     delete t;
     return rc;
   }
@@ -435,10 +455,14 @@ int ptg_tensor_create(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtyp
   return PTG_OK;
 }
 
+}  // namespace ptg
+
+extern "C" {
+
 int ptg_tensor_destroy(ptg_tensor *t) {
   if (!t) return PTG_OK;
   cudaSetDevice(t->device);
-  if (t->data) cudaFree(t->data);
+  if (t->data && t->owns) cudaFree(t->data);
   delete t;
   return PTG_OK;
 }

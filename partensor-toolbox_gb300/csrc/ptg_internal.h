@@ -73,6 +73,9 @@ struct ptg_ctx {
   int mttkrp_impl = 0;                // PTG_OPT_MTTKRP_IMPL
   int *dev_err = nullptr;             // device error word written by bounded waits
   std::map<std::string, int> tuned;   // autotuner choices (batched CPD split-K target)
+  // buffers of the one-call entry points (ptg_cpd, ptg_cpd_dimtree), kept between calls:
+  // the FP64 copy of the host tensor and the two stored tensors
+  ptg::DevBuf stage64, cache_x, cache_xr;
   void *pinned = nullptr;             // page-locked host staging, kept between calls
   size_t pinned_bytes = 0;
 };
@@ -86,6 +89,7 @@ struct ptg_tensor {
   void *data = nullptr;
   double frob64 = 0.0;      // ||X||^2 of the FP64 source
   double frob_stored = 0.0; // ||X||^2 of the stored copy
+  bool owns = true;         // false: data lives in a context-owned buffer
   int device = 0;
 };
 
@@ -159,6 +163,11 @@ int batched_plan(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, const 
                  int bn, int bm, int target_per_sm, BatchedContraction *bc);
 // active[inst] == 0 skips that instance's items (nullptr: all run).
 int batched_launch(ptg_ctx *ctx, const BatchedContraction &bc, const int *active, cudaStream_t stream);
+
+// ptg_tensor_create with the storage taken from `storage` (a context-owned buffer that
+// outlives the tensor) when it is not null.
+int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtype, const double *src,
+                       int src_on_device, DevBuf *storage, ptg_tensor **out);
 
 // Statistics helpers: count kernel launches; bracket a contraction with events.
 inline void count_launches(ptg_ctx *ctx, int n) { ctx->stats.launches += n; }
