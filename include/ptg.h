@@ -209,9 +209,10 @@ int ptg_cpd_als(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int
 
 /* One-call form with a HOST FP64 tensor: upload (with conversion to `dtype`), solve,
  * download.  This is what partensor::cpd(execution::cuda, tnsX, R, options, factorsInit)
- * (include/Cpd.hpp:1116-1144) binds to.  The device copy of the FP64 data and the stored
- * tensor(s) stay allocated in the context for the next call of the same or a smaller size
- * (ptg_ctx_destroy frees them). */
+ * (include/Cpd.hpp:1116-1144) binds to.  The host data streams through page-locked chunks
+ * (the copy of one chunk beside the conversion of the previous one) into the stored
+ * tensor(s), which stay allocated in the context for the next call of the same or a smaller
+ * size (ptg_ctx_destroy frees them). */
 int ptg_cpd(ptg_ctx *ctx, int order, const int64_t *dims, const double *host_tensor,
             ptg_dtype dtype, int rank, const ptg_cpd_options *opts,
             const double *const *init_factors, double *const *out_factors,

@@ -471,20 +471,13 @@ static int cpd_host_impl(ptg_ctx *ctx, int order, const int64_t *dims, const dou
   ptg_tensor *X = nullptr, *Xr = nullptr;
   const bool want_refine = dtype != PTG_F32 && (opts->refine_sweeps > 0 || opts->verify_fp32);
   int rc = PTG_OK;
-  // the FP64 copy and the stored tensors live in context-owned buffers kept for the next call
-  if (!want_refine) {
+  // the stored tensors live in context-owned buffers kept for the next call; the host data is
+  // streamed through page-locked chunks (copy of chunk k+1 beside the conversion of chunk k),
+  // and one pass writes both the BF16 tensor and its FP32 copy
+  if (!want_refine)
     rc = tensor_create_impl(ctx, order, dims, dtype, host_tensor, 0, &ctx->cache_x, &X);
-  } else {
-    // one host->device transfer of the FP64 data, two conversions on the device
-    int64_t numel = 1;
-    for (int k = 0; k < order; ++k) numel *= dims[k];
-    PTG_CUDA(cudaSetDevice(ctx->device));
-    PTG_TRY(ctx->stage64.ensure(sizeof(double) * numel));
-    double *dsrc = reinterpret_cast<double *>(ctx->stage64.ptr);
-    PTG_CUDA(cudaMemcpyAsync(dsrc, host_tensor, sizeof(double) * numel, cudaMemcpyHostToDevice, ctx->stream));
-    rc = tensor_create_impl(ctx, order, dims, dtype, dsrc, 1, &ctx->cache_x, &X);
-    if (rc == PTG_OK) rc = tensor_create_impl(ctx, order, dims, PTG_F32, dsrc, 1, &ctx->cache_xr, &Xr);
-  }
+  else
+    rc = tensor_create_impl(ctx, order, dims, dtype, host_tensor, 0, &ctx->cache_x, &X, &ctx->cache_xr, &Xr);
   if (rc == PTG_OK) rc = cpd_als_impl(ctx, X, Xr, rank, opts, init_factors, out_factors, result, trace, dimtree);
   ptg_tensor_destroy(X);
   ptg_tensor_destroy(Xr);

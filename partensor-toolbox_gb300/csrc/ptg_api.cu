@@ -112,12 +112,13 @@ namespace {
 
 // FP64 ColMajor source chunk -> padded storage, with FP64 partial sums of squares of the
 // source and of the stored values (one pair per block, summed later in block order).
+// the stored value of x (xf = (float)x, computed once): FP32 stores xf, BF16 rounds x directly
 template <typename T>
-__device__ __forceinline__ T cvt(double x);
+__device__ __forceinline__ T stored(double x, float xf);
 template <>
-__device__ __forceinline__ float cvt<float>(double x) { return (float)x; }
+__device__ __forceinline__ float stored<float>(double, float xf) { return xf; }
 template <>
-__device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16>(double x) { return __double2bfloat16(x); }
+__device__ __forceinline__ __nv_bfloat16 stored<__nv_bfloat16>(double x, float) { return __double2bfloat16(x); }
 __device__ __forceinline__ double back(float x) { return (double)x; }
 __device__ __forceinline__ double back(__nv_bfloat16 x) { return (double)__bfloat162float(x); }
 
@@ -127,24 +128,42 @@ constexpr int kConvThreads = 256;
 template <typename T>
 __global__ void __launch_bounds__(kConvThreads)
 convert_kernel(const double *__restrict__ src, int64_t I0, int64_t pI0, int64_t fiber0,
-               int64_t nfibers, T *__restrict__ dst, double *__restrict__ part) {
-  // element e of the padded chunk: i0 = e % pI0, fiber = e / pI0
-  const int64_t n = nfibers * pI0;
+               int64_t nfibers, T *__restrict__ dst, float *__restrict__ dst32, double *__restrict__ part) {
+  // a block per fibre (grid-stride over fibres), threads along i0: no index division.  The
+  // squares of four entries of a thread are summed in FP32 and then added in FP64 (the FP64
+  // pipe is the scarce one on this part; 4-entry FP32 partials keep ||X||^2 to ~1e-10
+  // relative)
   double s64 = 0.0, sst = 0.0;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i0 = e % pI0, f = e / pI0;
-    T v;
-    if (i0 < I0) {
-      const double x = src[f * I0 + i0];
-      v = cvt<T>(x);
-      s64 = fma(x, x, s64);
-      const double b = back(v);
-      sst = fma(b, b, sst);
-    } else {
-      v = cvt<T>(0.0);
+  for (int64_t f = blockIdx.x; f < nfibers; f += gridDim.x) {
+    const double *s = src + f * I0;
+    T *d = dst + (fiber0 + f) * pI0;
+    float *d32 = dst32 ? dst32 + (fiber0 + f) * pI0 : nullptr;   // optional FP32 copy
+    // four entries per thread per pass: their loads are in flight together
+    for (int64_t base = threadIdx.x; base < pI0; base += 4 * (int64_t)blockDim.x) {
+      double x[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t i0 = base + j * (int64_t)blockDim.x;
+        x[j] = i0 < I0 ? __ldcs(s + i0) : 0.0;
+      }
+      float p64 = 0.0f, pst = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t i0 = base + j * (int64_t)blockDim.x;
+        if (i0 < pI0) {
+          // one FP64 -> FP32 conversion per entry (it runs on the slow FP64 pipe)
+          const float xf = (float)x[j];
+          const T v = stored<T>(x[j], xf);   // pads (i0 >= I0) store zero
+          const float bf = (float)back(v);
+          p64 = fmaf(xf, xf, p64);
+          pst = fmaf(bf, bf, pst);
+          d[i0] = v;
+          if (d32) d32[i0] = xf;
+        }
+      }
+      s64 += (double)p64;
+      sst += (double)pst;
     }
-    dst[(fiber0 + f) * pI0 + i0] = v;
   }
   __shared__ double r64[kConvThreads / 32], rst[kConvThreads / 32];
   for (int o = 16; o > 0; o >>= 1) {
@@ -232,7 +251,6 @@ int ptg_ctx_destroy(ptg_ctx *c) {
   for (cudaEvent_t e : c->stats.pool) cudaEventDestroy(e);
   if (c->dev_err) cudaFree(c->dev_err);
   if (c->pinned) cudaFreeHost(c->pinned);
-  c->stage64.release();
   c->cache_x.release();
   c->cache_xr.release();
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
@@ -316,7 +334,7 @@ int ptg_ctx_reset_stats(ptg_ctx *c) {
 
 int ptg_tensor_create(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtype,
                       const double *src, int src_on_device, ptg_tensor **out) {
-  return ptg::tensor_create_impl(c, order, dims, dtype, src, src_on_device, nullptr, out);
+  return ptg::tensor_create_impl(c, order, dims, dtype, src, src_on_device, nullptr, out, nullptr, nullptr);
 }
 
 }  // extern "C"
@@ -324,9 +342,14 @@ int ptg_tensor_create(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtyp
 namespace ptg {
 
 int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtype, const double *src,
-                       int src_on_device, DevBuf *storage, ptg_tensor **out) {
+                       int src_on_device, DevBuf *storage, ptg_tensor **out, DevBuf *storage32,
+                       ptg_tensor **out32) {
   if (!c || !dims || !src || !out) return set_error(PTG_ERR_INVALID, "NULL argument");
   *out = nullptr;
+  if (out32) {
+    *out32 = nullptr;
+    if (dtype == PTG_F32) return set_error(PTG_ERR_INVALID, "internal: an FP32 copy beside an FP32 tensor");
+  }
   if (order < 2 || order > PTG_MAX_ORDER)
     return set_error(PTG_ERR_UNSUPPORTED, "tensor order must be in [2, 8]");
   if (dtype != PTG_F32 && dtype != PTG_BF16) return set_error(PTG_ERR_UNSUPPORTED, "dtype");
@@ -358,10 +381,34 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
     delete t;
     return cuda_error(e, "cudaMalloc(tensor)", __FILE__, __LINE__);
   }
+  // the optional FP32 copy, written by the same pass
+  ptg_tensor *t32 = nullptr;
+  if (out32) {
+    t32 = new ptg_tensor(*t);
+    t32->dtype = PTG_F32;
+    t32->owns = true;
+    int rs = PTG_OK;
+    if (storage32) {
+      rs = storage32->ensure((size_t)t->numel_padded * 4);
+      t32->data = storage32->ptr;
+      t32->owns = false;
+    } else if ((e = cudaMalloc(&t32->data, (size_t)t->numel_padded * 4)) != cudaSuccess) {
+      rs = cuda_error(e, "cudaMalloc(tensor)", __FILE__, __LINE__);
+    }
+    if (rs != PTG_OK) {
+      if (t->owns) cudaFree(t->data);
+      delete t;
+      delete t32;
+      return rs;
+    }
+  }
+  float *d32 = t32 ? (float *)t32->data : nullptr;
   const int64_t I0 = dims[0], pI0 = t->pdim0;
   const int64_t nfib = numel / I0;
   // staging for host sources: two chunk buffers, copies on `side`, conversion on `stream`
-  const int64_t chunk_fib = std::max<int64_t>(1, std::min<int64_t>(nfib, (64ll << 20) / I0));
+  // (a device source is converted in one launch; a host source streams through 64 MB chunks)
+  const int64_t chunk_fib =
+      src_on_device ? nfib : std::max<int64_t>(1, std::min<int64_t>(nfib, (64ll << 20) / I0));
   double *stage[2] = {nullptr, nullptr};
   double *part = nullptr, *acc = nullptr;
   cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
@@ -409,14 +456,13 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
         cudaStreamWaitEvent(c->stream, copied[b], 0);
         csrc = stage[b];
       }
-      const int64_t n = nf * pI0;
-      const int blocks = (int)std::min<int64_t>(kConvBlocks, (n + kConvThreads - 1) / kConvThreads);
+      const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(kConvBlocks, nf));
       if (dtype == PTG_F32)
         convert_kernel<float><<<blocks, kConvThreads, 0, c->stream>>>(
-            csrc, I0, pI0, f0, nf, (float *)t->data, part);
+            csrc, I0, pI0, f0, nf, (float *)t->data, nullptr, part);
       else
         convert_kernel<__nv_bfloat16><<<blocks, kConvThreads, 0, c->stream>>>(
-            csrc, I0, pI0, f0, nf, (__nv_bfloat16 *)t->data, part);
+            csrc, I0, pI0, f0, nf, (__nv_bfloat16 *)t->data, d32, part);
       sum_partials_kernel<<<1, 32, 0, c->stream>>>(part, blocks, acc);
       count_launches(c, 2);
       if (!src_on_device) cudaEventRecord(consumed[chunk_idx & 1], c->stream);
@@ -435,6 +481,7 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
     }
     t->frob64 = h[0];
     t->frob_stored = h[1];
+    if (t32) t32->frob64 = t32->frob_stored = h[0];   // the FP32 copy stores exactly the squared values summed
     if (!std::isfinite(h[0]) || !std::isfinite(h[1]))
       fail(set_error(PTG_ERR_NUMERIC, "tensor contains NaN or Inf"));
   } while (0);
@@ -447,11 +494,16 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
   if (part) cudaFree(part);
   if (acc) cudaFree(acc);
   if (rc != PTG_OK) {
+    if (t32) {
+      if (t32->owns) cudaFree(t32->data);
+      delete t32;
+    }
     if (t->owns) cudaFree(t->data);
     delete t;
     return rc;
   }
   *out = t;
+  if (out32) *out32 = t32;
   return PTG_OK;
 }
 

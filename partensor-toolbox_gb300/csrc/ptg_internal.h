@@ -74,8 +74,8 @@ struct ptg_ctx {
   int *dev_err = nullptr;             // device error word written by bounded waits
   std::map<std::string, int> tuned;   // autotuner choices (batched CPD split-K target)
   // buffers of the one-call entry points (ptg_cpd, ptg_cpd_dimtree), kept between calls:
-  // the FP64 copy of the host tensor and the two stored tensors
-  ptg::DevBuf stage64, cache_x, cache_xr;
+  // the stored tensor and its FP32 copy
+  ptg::DevBuf cache_x, cache_xr;
   void *pinned = nullptr;             // page-locked host staging, kept between calls
   size_t pinned_bytes = 0;
 };
@@ -165,9 +165,11 @@ int batched_plan(ptg_ctx *ctx, const std::vector<const ptg_tensor *> &ts, const 
 int batched_launch(ptg_ctx *ctx, const BatchedContraction &bc, const int *active, cudaStream_t stream);
 
 // ptg_tensor_create with the storage taken from `storage` (a context-owned buffer that
-// outlives the tensor) when it is not null.
+// outlives the tensor) when it is not null; with out32, the same pass over the source also
+// writes an FP32 copy (storage from storage32 when not null) beside a BF16 tensor.
 int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtype, const double *src,
-                       int src_on_device, DevBuf *storage, ptg_tensor **out);
+                       int src_on_device, DevBuf *storage, ptg_tensor **out, DevBuf *storage32 = nullptr,
+                       ptg_tensor **out32 = nullptr);
 
 // Statistics helpers: count kernel launches; bracket a contraction with events.
 inline void count_launches(ptg_ctx *ctx, int n) { ctx->stats.launches += n; }
