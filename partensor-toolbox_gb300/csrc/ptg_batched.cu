@@ -201,19 +201,21 @@ struct Carve {
 __global__ void __launch_bounds__(kUpThreads)
 upload_convert_kernel(const double *__restrict__ src, int64_t I0, int64_t pI0, int64_t f0, int64_t nf,
                       float *__restrict__ dst, double *__restrict__ part, unsigned *ticket, double *acc) {
-  const int64_t n = nf * pI0;
-  double s64 = 0.0, sst = 0.0;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i0 = e % pI0, f = e / pI0;
+  // a piece holds at most one staging chunk (64 MB), so 32-bit index arithmetic suffices; the
+  // squares are summed in FP32 per thread-step and added in FP64 (the FP64 pipe is the scarce
+  // one); the stored FP32 value's square is the source's square rounded the same way
+  const uint32_t n = (uint32_t)(nf * pI0), upI0 = (uint32_t)pI0, uI0 = (uint32_t)I0;
+  double s64 = 0.0;
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const uint32_t f = e / upI0, i0 = e - f * upI0;
     float v = 0.0f;
-    if (i0 < I0) {
-      const double x = src[f * I0 + i0];
-      v = (float)x;
-      s64 = fma(x, x, s64);
-      sst = fma((double)v, (double)v, sst);
+    if (i0 < uI0) {
+      v = (float)__ldcs(src + (size_t)f * uI0 + i0);
+      s64 += (double)(v * v);
     }
     dst[(f0 + f) * pI0 + i0] = v;
   }
+  double sst = s64;
   __shared__ double r64[kUpThreads / 32], rst[kUpThreads / 32];
   __shared__ bool last;
   for (int o = 16; o > 0; o >>= 1) {
@@ -436,15 +438,9 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
     PTG_CUDA(cudaStreamSynchronize(S));
   }
 
-  // ---- tensors: page-locked double buffer filled by host threads, one H2D per chunk, FP32
-  // conversion with FP64 ||X||^2 on the device ----
-  if (ctx->pinned_bytes < 2 * (size_t)kStageBytes) {
-    if (ctx->pinned) cudaFreeHost(ctx->pinned);
-    ctx->pinned = nullptr;
-    ctx->pinned_bytes = 0;
-    PTG_CUDA(cudaHostAlloc(&ctx->pinned, 2 * (size_t)kStageBytes, cudaHostAllocDefault));
-    ctx->pinned_bytes = 2 * (size_t)kStageBytes;
-  }
+  // ---- tensors: copied chunk by chunk into a device double buffer on the side stream, FP32
+  // conversion with FP64 ||X||^2 on the main stream (the copy of chunk k beside the conversion
+  // of chunk k-1) ----
   {
     struct Piece {
       int inst;
@@ -470,55 +466,38 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
         f0 += nf;
       }
     }
-    cudaEvent_t freed[2] = {nullptr, nullptr};
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};   // freed[2], copied[2]
     struct EvGuard {
       cudaEvent_t *e;
       ~EvGuard() {
-        for (int b = 0; b < 2; ++b)
+        for (int b = 0; b < 4; ++b)
           if (e[b]) cudaEventDestroy(e[b]);
       }
-    } evg{freed};
-    for (int b = 0; b < 2; ++b) PTG_CUDA(cudaEventCreateWithFlags(&freed[b], cudaEventDisableTiming));
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const int workers = (int)std::min<unsigned>(hw, 16u);
+    } evg{ev};
+    for (int b = 0; b < 4; ++b) PTG_CUDA(cudaEventCreateWithFlags(&ev[b], cudaEventDisableTiming));
+    cudaEvent_t *freed = ev, *copied = ev + 2;
     for (size_t ck = 0; ck < chunks.size(); ++ck) {
       const int b = (int)(ck & 1);
-      double *host = (double *)ctx->pinned + (size_t)b * stage_elems;
-      if (ck >= 2) PTG_CUDA(cudaEventSynchronize(freed[b]));
-      // copy tasks of at most 4 MiB
-      struct Task {
-        const double *src;
-        double *dst;
-        size_t n;
-      };
-      std::vector<Task> tasks;
-      size_t total = 0;
+      if (ck >= 2) PTG_CUDA(cudaStreamWaitEvent(side.s, freed[b], 0));
+      // the pieces are copied straight from the caller's buffers: on this host a pageable copy
+      // runs near the link's rate, so no page-locked bounce is needed
       for (const Piece &p : chunks[ck]) {
         const int64_t I0 = inst[p.inst].dims[0];
-        const double *src = inst[p.inst].tensor + p.f0 * I0;
-        const size_t n = (size_t)(p.nf * I0);
-        for (size_t o = 0; o < n; o += (size_t)1 << 19) tasks.push_back(Task{src + o, host + p.off + o, std::min(n - o, (size_t)1 << 19)});
-        total = std::max(total, p.off + n);
+        PTG_CUDA(cudaMemcpyAsync(d_stage[b] + p.off, inst[p.inst].tensor + p.f0 * I0,
+                                 sizeof(double) * (size_t)(p.nf * I0), cudaMemcpyHostToDevice, side.s));
       }
-      std::atomic<size_t> next{0};
-      auto work = [&] {
-        for (size_t t; (t = next.fetch_add(1)) < tasks.size();) std::memcpy(tasks[t].dst, tasks[t].src, tasks[t].n * sizeof(double));
-      };
-      std::vector<std::thread> pool;
-      const int nw = (int)std::min<size_t>((size_t)workers, tasks.size());
-      for (int w = 1; w < nw; ++w) pool.emplace_back(work);
-      work();
-      for (auto &th : pool) th.join();
-      PTG_CUDA(cudaMemcpyAsync(d_stage[b], host, total * sizeof(double), cudaMemcpyHostToDevice, S));
-      PTG_CUDA(cudaEventRecord(freed[b], S));
+      PTG_CUDA(cudaEventRecord(copied[b], side.s));
+      PTG_CUDA(cudaStreamWaitEvent(S, copied[b], 0));
       for (const Piece &p : chunks[ck]) {
         const int64_t I0 = inst[p.inst].dims[0], pI0 = Tst[p.inst].pdim0;
         upload_convert_kernel<<<kUpBlocks, kUpThreads, 0, S>>>(d_stage[b] + p.off, I0, pI0, p.f0, p.nf, Xdata[p.inst],
                                                                d_part, d_ticket, d_up + 2 * p.inst);
         count_launches(ctx, 1);
       }
+      PTG_CUDA(cudaEventRecord(freed[b], S));
       PTG_CUDA(cudaGetLastError());
     }
+    PTG_CUDA(cudaStreamSynchronize(side.s));
     std::vector<double> up(2 * (size_t)n_inst);
     PTG_CUDA(cudaMemcpyAsync(up.data(), d_up, sizeof(double) * up.size(), cudaMemcpyDeviceToHost, S));
     PTG_CUDA(cudaStreamSynchronize(S));
