@@ -15,6 +15,7 @@ PTG_OK, PTG_ERR_INVALID, PTG_ERR_CUDA, PTG_ERR_OOM, PTG_ERR_UNSUPPORTED, PTG_ERR
 PTG_F32, PTG_BF16 = 0, 1
 PTG_OPT_MTTKRP_IMPL = 1
 PTG_OPT_NNLS_CLUSTER = 2
+PTG_OPT_GTC_ROWS = 3
 MTTKRP_IMPLS = {"auto": 0, "cuda_cores": 1, "tensor_cores": 2}
 
 # every symbol include/ptg.h declares

@@ -109,6 +109,11 @@ class Context:
         """CTAs of the NNLS cluster: 0 (auto), 2, 4, 8 or 16."""
         check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_NNLS_CLUSTER, int(size)))
 
+    def set_gtc_rows(self, solver: str):
+        """Row solver of the stochastic sparse completion: "auto" (one warp per row for
+        rank <= 32) or "cta" (one CTA per row)."""
+        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_GTC_ROWS, {"auto": 0, "cta": 1}[solver]))
+
     def enable_stats(self, on: bool = True):
         check(self._lib.ptg_ctx_enable_stats(self.handle, int(on)))
 

@@ -286,6 +286,10 @@ int ptg_ctx_set_option(ptg_ctx *c, int option, long long value) {
         return set_error(PTG_ERR_INVALID, "NNLS cluster size must be 0 (auto), 2, 4, 8 or 16");
       c->nnls_cluster = (int)value;   // 0: probe again on the next solve
       return PTG_OK;
+    case PTG_OPT_GTC_ROWS:
+      if (value != 0 && value != 1) return set_error(PTG_ERR_INVALID, "GTC row solver must be 0 (auto) or 1");
+      c->gtc_rows = (int)value;
+      return PTG_OK;
     default:
       return set_error(PTG_ERR_INVALID, "unknown option");
   }

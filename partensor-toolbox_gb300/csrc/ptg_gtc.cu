@@ -11,7 +11,8 @@
 //   entries once, accumulates m_i = sum x kr and H_i = sum kr kr^T, runs PowerMethod on H_i
 //   and the max_nesterov_iter projected Nesterov steps with grad = H_i y - m_i + lambda y;
 //   dynamic_blocksize::StochasticNesterovMNLS (include/NesterovMNLS.hpp:431-547): the same per
-//   row on a contiguous block of floor(c * nnz_i) entries at a counter-hashed pivot;
+//   row on a contiguous block of floor(c * nnz_i) entries at a counter-hashed pivot, one warp
+//   per row at rank <= 32 (H_i in registers, no CTA barrier), else one CTA per row;
 //   the GTC cost (include/Gtc.hpp:184-214) as per-row FP64 partial sums added in row order.
 // No global atomics on the data path; every reduction is in a fixed order.
 #include <algorithm>
@@ -397,7 +398,7 @@ __device__ float power_method_warp(RowShared &sh, int R, float eps) {
     for (int q = 0; q < 2; ++q) {
       const int r = lane + 32 * q;
       if (r < R) {
-        const float xn = ax[q] * inv;
+        const float xn = __fmul_rn(ax[q], inv);   // kept out of an FMA with the difference
         const float df = xn - sh.x[r];
         d2 += df * df;
         sh.xn[r] = xn;
@@ -465,6 +466,21 @@ __device__ void ridge_solve_warp(RowShared &sh, int R, float lam, int *err) {
   if (bad && lane == 0) atomicExch(err, PTG_ERR_NUMERIC);
 }
 
+// The scalar parts of one projected Nesterov step (include/NesterovMNLS.hpp:525-539, :855-864), with
+// explicit FMAs so that the one-CTA and the one-warp row kernels round them alike.
+__device__ __forceinline__ float step_grad0(float m, float lam, float y, float prox, float a) {
+  return fmaf(lam, fmaf(prox, a, y), -m);   // -m + lambda (y + prox a)
+}
+__device__ __forceinline__ float step_project(float y, float invL, float g) { return fmaxf(fmaf(-invL, g, y), 0.0f); }
+__device__ __forceinline__ float step_extrapolate(float beta, float na, float a) {
+  return fmaf(1.0f + beta, na, -(beta * a));
+}
+__device__ __forceinline__ void step_constants(float lmax, float lam, float &invL, float &beta) {
+  invL = 1.0f / (lmax + lam);
+  const float sq = sqrtf(lam * invL);
+  beta = (1.0f - sq) / (1.0f + sq);
+}
+
 // One projected Nesterov step of warp 0: grad = H y - m + lambda * (y + prox * a_prev)
 __device__ void nesterov_step_warp(RowShared &sh, int R, float lam, float invL, float beta, float prox) {
   const int lane = threadIdx.x & 31;
@@ -473,16 +489,16 @@ __device__ void nesterov_step_warp(RowShared &sh, int R, float lam, float invL, 
     const int r = lane + 32 * q;
     na[q] = 0.f;
     if (r < R) {
-      float g = -sh.m[r] + lam * (sh.y[r] + prox * sh.a[r]);
+      float g = step_grad0(sh.m[r], lam, sh.y[r], prox, sh.a[r]);
       for (int c = 0; c < R; ++c) g = fmaf(sh.H[r][c], sh.y[c], g);
-      na[q] = fmaxf(sh.y[r] - invL * g, 0.0f);
+      na[q] = step_project(sh.y[r], invL, g);
     }
   }
   __syncwarp();
   for (int q = 0; q < 2; ++q) {
     const int r = lane + 32 * q;
     if (r < R) {
-      sh.y[r] = (1.0f + beta) * na[q] - beta * sh.a[r];
+      sh.y[r] = step_extrapolate(beta, na[q], sh.a[r]);
       sh.a[r] = na[q];
     }
   }
@@ -518,17 +534,13 @@ __global__ void __launch_bounds__(GT_THREADS) gtc_row_kernel(const RowArgs a) {
     if (a.ridge) {
       if (tid < 32) ridge_solve_warp(sh, R, a.lambda, a.err);   // an empty row gives a_i = 0
     } else if (tid < 32 && cnt_row > 0) {
-      const float L = power_method_warp(sh, R, 1e-3f) + a.lambda;
-      const float invL = 1.0f / L;
-      const float sq = sqrtf(a.lambda * invL);
-      const float beta = (1.0f - sq) / (1.0f + sq);
+      float invL, beta;
+      step_constants(power_method_warp(sh, R, 1e-3f), a.lambda, invL, beta);
       for (int it = 0; it < a.max_iter; ++it) nesterov_step_warp(sh, R, a.lambda, invL, beta, 0.0f);
     } else if (tid < 32) {
       // an empty row: H = 0, m = 0, L = lambda; the steps only shrink the row
-      const float L = a.lambda;
-      const float invL = 1.0f / L;
-      const float sq = sqrtf(a.lambda * invL);
-      const float beta = (1.0f - sq) / (1.0f + sq);
+      float invL, beta;
+      step_constants(0.0f, a.lambda, invL, beta);
       for (int it = 0; it < a.max_iter; ++it) nesterov_step_warp(sh, R, a.lambda, invL, beta, 0.0f);
     }
   } else {
@@ -555,10 +567,8 @@ __global__ void __launch_bounds__(GT_THREADS) gtc_row_kernel(const RowArgs a) {
         __syncthreads();
         if (tid < 32) {
           // grad = sum (kr.y - x) kr + lambda (y + a) = H y - m + lambda (y + a)  (:516, :525)
-          const float L = power_method_warp(sh, R, 1e-3f) + a.lambda;
-          const float invL = 1.0f / L;
-          const float sq = sqrtf(a.lambda * invL);
-          const float beta = (1.0f - sq) / (1.0f + sq);
+          float invL, beta;
+          step_constants(power_method_warp(sh, R, 1e-3f), a.lambda, invL, beta);
           nesterov_step_warp(sh, R, a.lambda, invL, beta, 1.0f);
         }
         __syncthreads();
@@ -587,6 +597,138 @@ __global__ void __launch_bounds__(GT_THREADS) gtc_row_kernel(const RowArgs a) {
       a.row_cost[i] = t;
     }
   }
+}
+
+// ---- one warp per row (rank <= 32): dynamic_blocksize::StochasticNesterovMNLS ----
+// The one-CTA kernel keeps three of its four warps waiting at barriers while warp 0 runs the
+// power method and the step.  Here each warp owns a row: lane r holds row r of the sampled H_i
+// in registers (H is symmetric, so it is also column r), m_i[r], a_i[r] and the extrapolated
+// y[r]; a vector every lane needs (a Khatri-Rao row, the power iterate, y) passes through the
+// warp's own shared-memory slots, and only __syncwarp orders them.  The arithmetic and its
+// order are those of the one-CTA kernel, so the two give the same bits.  64 registers (8 CTAs,
+// 32 warps per SM, a few bytes spilled) measured faster than 92 without spills (20 warps).
+constexpr int GW_WARPS = 4;
+constexpr int GW_CHUNK = 32;
+
+struct WarpRowShared {
+  float kr[GW_CHUNK][32];
+  float xv[GW_CHUNK];
+  float v[32];
+  int32_t rows[PTG_MAX_ORDER - 1][GW_CHUNK];
+};
+
+__device__ __forceinline__ float warp_sum(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// s + (H v)[lane], the products added in increasing column order
+__device__ __forceinline__ float row_dot(const float (&H)[32], const float *v, float s) {
+  const float4 *v4 = reinterpret_cast<const float4 *>(v);
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const float4 t = v4[q];
+    s = fmaf(H[4 * q], t.x, s);
+    s = fmaf(H[4 * q + 1], t.y, s);
+    s = fmaf(H[4 * q + 2], t.z, s);
+    s = fmaf(H[4 * q + 3], t.w, s);
+  }
+  return s;
+}
+
+// power_method_warp with the matrix in the lanes' registers
+__device__ __forceinline__ float power_method_lane(const float (&H)[32], float *v, bool own, float eps) {
+  const int lane = threadIdx.x & 31;
+  float x = own ? 1.0f : 0.0f;
+  v[lane] = x;
+  __syncwarp();
+  for (int it = 0;; ++it) {
+    const float s = row_dot(H, v, 0.0f);
+    const float nrm2 = warp_sum(s * s);
+    const float inv = 1.0f / (sqrtf(nrm2) + 1e-12f);
+    const float xn = __fmul_rn(s, inv);
+    const float df = xn - x;
+    const float d2 = warp_sum(df * df);
+    __syncwarp();
+    v[lane] = xn;
+    __syncwarp();
+    if (sqrtf(d2) <= eps || it >= 10000) {
+      const float q2 = warp_sum(xn * row_dot(H, v, 0.0f));
+      __syncwarp();
+      return q2;
+    }
+    x = xn;
+  }
+}
+
+__global__ void __launch_bounds__(GW_WARPS * 32, 8) gtc_stoch_warp_kernel(const RowArgs a, int64_t rows) {
+  __shared__ __align__(16) WarpRowShared shw[GW_WARPS];
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * GW_WARPS + (threadIdx.x >> 5);
+  if (i >= rows) return;   // whole warps leave: the kernel has no CTA-wide barrier
+  WarpRowShared &sh = shw[threadIdx.x >> 5];
+  const int R = a.R, nj = a.N - 1;
+  const bool own = lane < R;
+  const int64_t p0 = a.ptr[i], cnt_row = a.ptr[i + 1] - p0;
+  float av = own ? a.A[i * R + lane] : 0.0f;
+  float yv = av;
+  const int64_t b = (int64_t)(a.c * (float)cnt_row);   // floor(c * nnz_i)
+  if (b > 0) {
+    for (int it = 0; it < a.max_iter; ++it) {
+      const unsigned long long draw = splitmix_draw(a.seed, (unsigned long long)a.outer,
+                                                    (unsigned long long)a.mode, (unsigned long long)it,
+                                                    (unsigned long long)i);
+      const int64_t s1 = p0 + (int64_t)(draw % (unsigned long long)(cnt_row - b + 1));
+      float H[32];
+#pragma unroll
+      for (int c = 0; c < 32; ++c) H[c] = 0.0f;
+      float m = 0.0f;
+      for (int64_t s0 = s1; s0 < s1 + b; s0 += GW_CHUNK) {
+        const int cnt = (int)(s1 + b - s0 < GW_CHUNK ? s1 + b - s0 : GW_CHUNK);
+        // lane e reads entry e's rows in the other modes and its value
+        if (lane < cnt) {
+          for (int j = 0; j < nj; ++j) sh.rows[j][lane] = a.oidx[(int64_t)j * a.nnz + s0 + lane];
+          sh.xv[lane] = a.vals[s0 + lane];
+        }
+        __syncwarp();
+        // each entry's Khatri-Rao row, the product taken from the last mode down (kr_value)
+#pragma unroll 4
+        for (int e = 0; e < cnt; ++e) {
+          float kv = 1.0f;
+#pragma unroll
+          for (int j = PTG_MAX_ORDER - 2; j >= 0; --j)
+            if (j < nj) kv *= own ? __ldg(a.fac[j] + (size_t)sh.rows[j][e] * R + lane) : 0.0f;
+          sh.kr[e][lane] = kv;
+        }
+        __syncwarp();
+        for (int e = 0; e < cnt; ++e) {
+          const float ke = sh.kr[e][lane];
+          const float4 *k4 = reinterpret_cast<const float4 *>(sh.kr[e]);
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const float4 t = k4[q];
+            H[4 * q] = fmaf(ke, t.x, H[4 * q]);
+            H[4 * q + 1] = fmaf(ke, t.y, H[4 * q + 1]);
+            H[4 * q + 2] = fmaf(ke, t.z, H[4 * q + 2]);
+            H[4 * q + 3] = fmaf(ke, t.w, H[4 * q + 3]);
+          }
+          m = fmaf(sh.xv[e], ke, m);
+        }
+        __syncwarp();
+      }
+      float invL, beta;
+      step_constants(power_method_lane(H, sh.v, own, 1e-3f), a.lambda, invL, beta);
+      // grad = H y - m + lambda (y + a) (include/NesterovMNLS.hpp:516, :525)
+      sh.v[lane] = yv;
+      __syncwarp();
+      const float g = row_dot(H, sh.v, step_grad0(m, a.lambda, yv, 1.0f, av));
+      const float na = own ? step_project(yv, invL, g) : 0.0f;
+      __syncwarp();
+      yv = step_extrapolate(beta, na, av);
+      av = na;
+    }
+  }
+  if (own) a.A[i * R + lane] = av;
 }
 
 // Cost of the current factors over one mode's entries (rows of that mode), per row.
@@ -920,7 +1062,10 @@ int ptg_gtc(ptg_ctx *ctx, int order, const int64_t *dims, int64_t nnz, const int
       RowArgs a = make_args(n);
       a.outer = ao_iter;
       a.ridge = ridge ? 1 : 0;
-      gtc_row_kernel<<<(unsigned)dims[n], GT_THREADS, smem, S>>>(a);
+      if (opt->stochastic && R <= 32 && ctx->gtc_rows == 0)
+        gtc_stoch_warp_kernel<<<(unsigned)((dims[n] + GW_WARPS - 1) / GW_WARPS), GW_WARPS * 32, 0, S>>>(a, dims[n]);
+      else
+        gtc_row_kernel<<<(unsigned)dims[n], GT_THREADS, smem, S>>>(a);
       count_launches(ctx, 1);
       PTG_CUDA(cudaGetLastError());
     }

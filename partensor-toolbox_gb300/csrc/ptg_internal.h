@@ -71,6 +71,7 @@ struct ptg_ctx {
   int nnls_cluster = 0;               // cluster size the NNLS kernel launched with (0 = unknown)
   ptg_ctx_stats stats;
   int mttkrp_impl = 0;                // PTG_OPT_MTTKRP_IMPL
+  int gtc_rows = 0;                   // PTG_OPT_GTC_ROWS
   int *dev_err = nullptr;             // device error word written by bounded waits
   std::map<std::string, int> tuned;   // autotuner choices (batched CPD split-K target)
   // buffers of the one-call entry points (ptg_cpd, ptg_cpd_dimtree), kept between calls:

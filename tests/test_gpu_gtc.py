@@ -117,3 +117,46 @@ def test_gtc_stochastic_keeps_unconstrained_modes(pkg, ctx):
     st = pkg.gtc_coo(idx, vals, o, stochastic=True, ctx=ctx)
     assert np.allclose(st.factors[1], init[1], atol=1e-7)
     assert not np.allclose(st.factors[0], init[0], atol=1e-3)
+
+
+@pytest.mark.parametrize("R", [3, 17, 32])
+def test_gtc_stochastic_row_solvers_agree(pkg, ctx, R):
+    """The stochastic row solver with one warp per row (rank <= 32: H_i in the lanes' registers)
+    and the one with one CTA per row do the same arithmetic in the same order: same bits."""
+    dims = (70, 60, 50)
+    idx, vals, init = _problem(dims, 30000, R, 21)
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=2, c_stochastic_perc=0.05,
+                          lambdas=[1e-3] * 3, seed=3, factorsInit=init)
+    out = {}
+    for solver in ("auto", "cta"):
+        c = pkg.Context(0)
+        try:
+            c.set_gtc_rows(solver)
+            out[solver] = pkg.gtc_coo(idx, vals, o, stochastic=True, ctx=c)
+        finally:
+            c.close()
+    for k in range(3):
+        assert np.array_equal(out["auto"].factors[k], out["cta"].factors[k]), k
+    assert out["auto"].rel_costFunction == out["cta"].rel_costFunction
+
+
+@pytest.mark.parametrize("R", [32, 40])
+def test_gtc_stochastic_matches_oracle_rank(pkg, ctx, R):
+    """Stochastic form at rank 32 (one warp per row) and 40 (one CTA per row) against the oracle.
+    Each sampled block holds >= 150 entries (> R), so the row problems are well posed: the oracle
+    moves by < 1e-7 under a 1e-6 perturbation of its initial factors here, while 30-entry blocks
+    at rank 32 move it by 5e-3 and say nothing about the kernel."""
+    dims = (40, 30, 20)
+    idx, vals, init = _problem(dims, 20000, R, 23)
+    c = 0.3
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=2, c_stochastic_perc=c,
+                          lambdas=[1e-2] * 3, seed=5, factorsInit=init)
+    st = pkg.gtc_coo(idx, vals, o, stochastic=True, ctx=ctx)
+    ref = og.gtc_stochastic(idx, vals, dims, R,
+                            og.SparseOptions(order=3, max_iter=2, c_stochastic_perc=c, lambdas=[1e-2] * 3,
+                                             seed=5), init)
+    assert st.ao_iter == ref.ao_iter
+    rel_gpu = np.array([t["rel"] for t in st.trace])
+    rel_ref = np.array([t["rel"] for t in ref.trace])
+    assert np.max(np.abs(rel_gpu - rel_ref)) < 2e-4, (rel_gpu, rel_ref)
+    assert oc.congruence(st.factors, ref.factors) >= 0.99
