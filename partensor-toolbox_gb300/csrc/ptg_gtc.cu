@@ -661,13 +661,17 @@ __device__ __forceinline__ float power_method_lane(const float (&H)[32], float *
   }
 }
 
+// NJ = order - 1 other modes; VEC: R is a multiple of 4, so every factor row starts on a
+// 16-byte boundary and 8 lanes gather one entry's Khatri-Rao row as float4s (4 entries per
+// warp instruction); otherwise lane r gathers rank r of one entry at a time.
+template <int NJ, bool VEC>
 __global__ void __launch_bounds__(GW_WARPS * 32, 8) gtc_stoch_warp_kernel(const RowArgs a, int64_t rows) {
   __shared__ __align__(16) WarpRowShared shw[GW_WARPS];
   const int lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * GW_WARPS + (threadIdx.x >> 5);
   if (i >= rows) return;   // whole warps leave: the kernel has no CTA-wide barrier
   WarpRowShared &sh = shw[threadIdx.x >> 5];
-  const int R = a.R, nj = a.N - 1;
+  const int R = a.R;
   const bool own = lane < R;
   const int64_t p0 = a.ptr[i], cnt_row = a.ptr[i + 1] - p0;
   float av = own ? a.A[i * R + lane] : 0.0f;
@@ -687,18 +691,42 @@ __global__ void __launch_bounds__(GW_WARPS * 32, 8) gtc_stoch_warp_kernel(const 
         const int cnt = (int)(s1 + b - s0 < GW_CHUNK ? s1 + b - s0 : GW_CHUNK);
         // lane e reads entry e's rows in the other modes and its value
         if (lane < cnt) {
-          for (int j = 0; j < nj; ++j) sh.rows[j][lane] = a.oidx[(int64_t)j * a.nnz + s0 + lane];
+#pragma unroll
+          for (int j = 0; j < NJ; ++j) sh.rows[j][lane] = a.oidx[(int64_t)j * a.nnz + s0 + lane];
           sh.xv[lane] = a.vals[s0 + lane];
         }
         __syncwarp();
-        // each entry's Khatri-Rao row, the product taken from the last mode down (kr_value)
-#pragma unroll 4
-        for (int e = 0; e < cnt; ++e) {
-          float kv = 1.0f;
+        // each entry's Khatri-Rao row, the product taken from the last mode down (kr_value);
+        // ranks >= R are zero
+        if (VEC) {
+          const int sub = lane >> 3, r4 = (lane & 7) * 4;
+#pragma unroll 2
+          for (int e = sub; e < cnt; e += 4) {
+            float4 kv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (r4 < R) {
+              kv = __ldg(reinterpret_cast<const float4 *>(a.fac[NJ - 1] + (size_t)sh.rows[NJ - 1][e] * R + r4));
 #pragma unroll
-          for (int j = PTG_MAX_ORDER - 2; j >= 0; --j)
-            if (j < nj) kv *= own ? __ldg(a.fac[j] + (size_t)sh.rows[j][e] * R + lane) : 0.0f;
-          sh.kr[e][lane] = kv;
+              for (int j = NJ - 2; j >= 0; --j) {
+                const float4 f = __ldg(reinterpret_cast<const float4 *>(a.fac[j] + (size_t)sh.rows[j][e] * R + r4));
+                kv.x *= f.x;
+                kv.y *= f.y;
+                kv.z *= f.z;
+                kv.w *= f.w;
+              }
+            }
+            *reinterpret_cast<float4 *>(&sh.kr[e][r4]) = kv;
+          }
+        } else {
+#pragma unroll 4
+          for (int e = 0; e < cnt; ++e) {
+            float kv = 0.0f;
+            if (own) {
+              kv = __ldg(a.fac[NJ - 1] + (size_t)sh.rows[NJ - 1][e] * R + lane);
+#pragma unroll
+              for (int j = NJ - 2; j >= 0; --j) kv *= __ldg(a.fac[j] + (size_t)sh.rows[j][e] * R + lane);
+            }
+            sh.kr[e][lane] = kv;
+          }
         }
         __syncwarp();
         for (int e = 0; e < cnt; ++e) {
@@ -729,6 +757,27 @@ __global__ void __launch_bounds__(GW_WARPS * 32, 8) gtc_stoch_warp_kernel(const 
     }
   }
   if (own) a.A[i * R + lane] = av;
+}
+
+template <int NJ>
+void launch_stoch_warp_nj(const RowArgs &a, int64_t rows, cudaStream_t S) {
+  const unsigned grid = (unsigned)((rows + GW_WARPS - 1) / GW_WARPS);
+  if (a.R % 4 == 0)
+    gtc_stoch_warp_kernel<NJ, true><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+  else
+    gtc_stoch_warp_kernel<NJ, false><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+}
+
+void launch_stoch_warp(const RowArgs &a, int64_t rows, cudaStream_t S) {
+  switch (a.N - 1) {
+    case 1: launch_stoch_warp_nj<1>(a, rows, S); break;
+    case 2: launch_stoch_warp_nj<2>(a, rows, S); break;
+    case 3: launch_stoch_warp_nj<3>(a, rows, S); break;
+    case 4: launch_stoch_warp_nj<4>(a, rows, S); break;
+    case 5: launch_stoch_warp_nj<5>(a, rows, S); break;
+    case 6: launch_stoch_warp_nj<6>(a, rows, S); break;
+    default: launch_stoch_warp_nj<7>(a, rows, S); break;
+  }
 }
 
 // Cost of the current factors over one mode's entries (rows of that mode), per row.
@@ -1063,7 +1112,7 @@ int ptg_gtc(ptg_ctx *ctx, int order, const int64_t *dims, int64_t nnz, const int
       a.outer = ao_iter;
       a.ridge = ridge ? 1 : 0;
       if (opt->stochastic && R <= 32 && ctx->gtc_rows == 0)
-        gtc_stoch_warp_kernel<<<(unsigned)((dims[n] + GW_WARPS - 1) / GW_WARPS), GW_WARPS * 32, 0, S>>>(a, dims[n]);
+        launch_stoch_warp(a, dims[n], S);
       else
         gtc_row_kernel<<<(unsigned)dims[n], GT_THREADS, smem, S>>>(a);
       count_launches(ctx, 1);
