@@ -605,13 +605,16 @@ __global__ void __launch_bounds__(GT_THREADS) gtc_row_kernel(const RowArgs a) {
 // in registers (H is symmetric, so it is also column r), m_i[r], a_i[r] and the extrapolated
 // y[r]; a vector every lane needs (a Khatri-Rao row, the power iterate, y) passes through the
 // warp's own shared-memory slots, and only __syncwarp orders them.  The arithmetic and its
-// order are those of the one-CTA kernel, so the two give the same bits.  64 registers (8 CTAs,
-// 32 warps per SM, a few bytes spilled) measured faster than 92 without spills (20 warps).
+// order are those of the one-CTA kernel, so the two give the same bits.  72 registers (7 CTAs,
+// 28 warps per SM, a few bytes spilled) measured faster than 64 (8 CTAs, more spilled) and than
+// 92 without spills (5 CTAs).
 constexpr int GW_WARPS = 4;
 constexpr int GW_CHUNK = 32;
 
+constexpr int GW_KRS = 36;   // row stride of the Khatri-Rao staging (16-byte rows, rotated banks)
+
 struct WarpRowShared {
-  float kr[GW_CHUNK][32];
+  float kr[GW_CHUNK][GW_KRS];   // one entry's Khatri-Rao row per row; after a block, H_i by rows
   float xv[GW_CHUNK];
   float v[32];
   int32_t rows[PTG_MAX_ORDER - 1][GW_CHUNK];
@@ -665,7 +668,7 @@ __device__ __forceinline__ float power_method_lane(const float (&H)[32], float *
 // 16-byte boundary and 8 lanes gather one entry's Khatri-Rao row as float4s (4 entries per
 // warp instruction); otherwise lane r gathers rank r of one entry at a time.
 template <int NJ, bool VEC>
-__global__ void __launch_bounds__(GW_WARPS * 32, 8) gtc_stoch_warp_kernel(const RowArgs a, int64_t rows) {
+__global__ void __launch_bounds__(GW_WARPS * 32, 7) gtc_stoch_warp_kernel(const RowArgs a, int64_t rows) {
   __shared__ __align__(16) WarpRowShared shw[GW_WARPS];
   const int lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * GW_WARPS + (threadIdx.x >> 5);
@@ -683,10 +686,16 @@ __global__ void __launch_bounds__(GW_WARPS * 32, 8) gtc_stoch_warp_kernel(const 
                                                     (unsigned long long)a.mode, (unsigned long long)it,
                                                     (unsigned long long)i);
       const int64_t s1 = p0 + (int64_t)(draw % (unsigned long long)(cnt_row - b + 1));
-      float H[32];
+      // lane (rg, cg) = (lane / 4, lane % 4) accumulates the 4 x 8 block of H_i at rows 4 rg..,
+      // columns 8 cg..: 3 float4 reads per entry for 32 FMAs, where a whole row per lane needs 8
+      // broadcast reads and shared memory, not the FMA pipe, sets the pace
+      const int rg = lane >> 2, cg = lane & 3;
+      float Hb[4][8];
 #pragma unroll
-      for (int c = 0; c < 32; ++c) H[c] = 0.0f;
-      float m = 0.0f;
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) Hb[k][j] = 0.0f;
+      float m4[4] = {0.0f, 0.0f, 0.0f, 0.0f};   // m_i at rows 4 rg.. (the 4 lanes of a row group alike)
       for (int64_t s0 = s1; s0 < s1 + b; s0 += GW_CHUNK) {
         const int cnt = (int)(s1 + b - s0 < GW_CHUNK ? s1 + b - s0 : GW_CHUNK);
         // lane e reads entry e's rows in the other modes and its value
@@ -729,21 +738,46 @@ __global__ void __launch_bounds__(GW_WARPS * 32, 8) gtc_stoch_warp_kernel(const 
           }
         }
         __syncwarp();
+#pragma unroll 2
         for (int e = 0; e < cnt; ++e) {
-          const float ke = sh.kr[e][lane];
-          const float4 *k4 = reinterpret_cast<const float4 *>(sh.kr[e]);
+          const float4 ra = *reinterpret_cast<const float4 *>(&sh.kr[e][4 * rg]);
+          const float rk[4] = {ra.x, ra.y, ra.z, ra.w};
+          const float xe = sh.xv[e];
 #pragma unroll
-          for (int q = 0; q < 8; ++q) {
-            const float4 t = k4[q];
-            H[4 * q] = fmaf(ke, t.x, H[4 * q]);
-            H[4 * q + 1] = fmaf(ke, t.y, H[4 * q + 1]);
-            H[4 * q + 2] = fmaf(ke, t.z, H[4 * q + 2]);
-            H[4 * q + 3] = fmaf(ke, t.w, H[4 * q + 3]);
+          for (int k = 0; k < 4; ++k) m4[k] = fmaf(xe, rk[k], m4[k]);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float4 cb = *reinterpret_cast<const float4 *>(&sh.kr[e][8 * cg + 4 * h]);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              Hb[k][4 * h] = fmaf(rk[k], cb.x, Hb[k][4 * h]);
+              Hb[k][4 * h + 1] = fmaf(rk[k], cb.y, Hb[k][4 * h + 1]);
+              Hb[k][4 * h + 2] = fmaf(rk[k], cb.z, Hb[k][4 * h + 2]);
+              Hb[k][4 * h + 3] = fmaf(rk[k], cb.w, Hb[k][4 * h + 3]);
+            }
           }
-          m = fmaf(sh.xv[e], ke, m);
         }
         __syncwarp();
       }
+      // H_i to one row per lane (row r in lane r) through the staging buffer
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          *reinterpret_cast<float4 *>(&sh.kr[4 * rg + k][8 * cg + 4 * h]) =
+              make_float4(Hb[k][4 * h], Hb[k][4 * h + 1], Hb[k][4 * h + 2], Hb[k][4 * h + 3]);
+      __syncwarp();
+      float H[32];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float4 t = *reinterpret_cast<const float4 *>(&sh.kr[lane][4 * q]);
+        H[4 * q] = t.x;
+        H[4 * q + 1] = t.y;
+        H[4 * q + 2] = t.z;
+        H[4 * q + 3] = t.w;
+      }
+      __syncwarp();   // the staging buffer is gathered into again by the next block
+      const float m = cg == 0 ? m4[0] : cg == 1 ? m4[1] : cg == 2 ? m4[2] : m4[3];   // m_i[lane]
       float invL, beta;
       step_constants(power_method_lane(H, sh.v, own, 1e-3f), a.lambda, invL, beta);
       // grad = H y - m + lambda (y + a) (include/NesterovMNLS.hpp:516, :525)
