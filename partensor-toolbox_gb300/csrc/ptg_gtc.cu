@@ -302,6 +302,7 @@ __device__ unsigned long long splitmix_draw(unsigned long long seed, unsigned lo
 struct RowShared {
   float kr[GT_CHUNK][GT_MAXR];
   float xv[GT_CHUNK];
+  int32_t rows[PTG_MAX_ORDER - 1][GT_CHUNK];   // the chunk's entries' rows in the other modes
   float H[GT_MAXR][GT_MAXR + 1];
   float m[GT_MAXR];
   float x[GT_MAXR], xn[GT_MAXR];
@@ -365,13 +366,51 @@ __device__ void tiles_store(RowShared &sh, int R, float (*acc)[8], float macc) {
   if ((int)threadIdx.x < R) sh.m[threadIdx.x] = macc;
 }
 
+// Stage a chunk of entries: their rows in the other modes and values, then each entry's
+// Khatri-Rao row (the product from the last mode down, as kr_value), zero beyond R.  The row
+// indices go through shared memory first, so that the factor loads of a chunk are independent
+// and in flight together (float4s where R is a multiple of 4).  Ends with a CTA barrier.
 __device__ void load_chunk(const RowArgs &a, RowShared &sh, int64_t s0, int cnt) {
-  const int Rp = (a.R + 3) & ~3;
-  for (int idx = threadIdx.x; idx < cnt * Rp; idx += GT_THREADS) {
-    const int c = idx / Rp, r = idx % Rp;
-    sh.kr[c][r] = r < a.R ? kr_value(a, s0 + c, r) : 0.0f;
+  const int R = a.R, Rp = (R + 3) & ~3, nj = a.N - 1;
+  for (int idx = threadIdx.x; idx < cnt * nj; idx += GT_THREADS) {
+    const int j = idx / cnt, c = idx - j * cnt;
+    sh.rows[j][c] = a.oidx[(int64_t)j * a.nnz + s0 + c];
   }
   for (int c = threadIdx.x; c < cnt; c += GT_THREADS) sh.xv[c] = a.vals[s0 + c];
+  __syncthreads();
+  if ((R & 3) == 0) {
+    const int q4 = R >> 2;
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < cnt * q4; idx += GT_THREADS) {
+      const int c = idx / q4, r4 = (idx - c * q4) * 4;
+      float4 v = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+#pragma unroll
+      for (int j = PTG_MAX_ORDER - 2; j >= 0; --j) {
+        if (j < nj) {
+          const float4 f = __ldg(reinterpret_cast<const float4 *>(a.fac[j] + (size_t)sh.rows[j][c] * R + r4));
+          v.x *= f.x;
+          v.y *= f.y;
+          v.z *= f.z;
+          v.w *= f.w;
+        }
+      }
+      *reinterpret_cast<float4 *>(&sh.kr[c][r4]) = v;
+    }
+  } else {
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < cnt * Rp; idx += GT_THREADS) {
+      const int c = idx / Rp, r = idx - c * Rp;
+      float v = 0.0f;
+      if (r < R) {
+        v = 1.0f;
+#pragma unroll
+        for (int j = PTG_MAX_ORDER - 2; j >= 0; --j)
+          if (j < nj) v *= __ldg(a.fac[j] + (size_t)sh.rows[j][c] * R + r);
+      }
+      sh.kr[c][r] = v;
+    }
+  }
+  __syncthreads();
 }
 
 // Power method of include/NesterovMNLS.hpp:131-160 on sh.H from the all-ones vector, by warp 0.
@@ -525,7 +564,6 @@ __global__ void __launch_bounds__(GT_THREADS) gtc_row_kernel(const RowArgs a) {
     for (int64_t s0 = p0; s0 < p1; s0 += GT_CHUNK) {
       const int cnt = (int)(p1 - s0 < GT_CHUNK ? p1 - s0 : GT_CHUNK);
       load_chunk(a, sh, s0, cnt);
-      __syncthreads();
       accumulate_chunk(sh, cnt, R, acc, macc);
       __syncthreads();
     }
@@ -559,7 +597,6 @@ __global__ void __launch_bounds__(GT_THREADS) gtc_row_kernel(const RowArgs a) {
         for (int64_t s0 = p0 + pivot; s0 < p0 + pivot + b; s0 += GT_CHUNK) {
           const int cnt = (int)(p0 + pivot + b - s0 < GT_CHUNK ? p0 + pivot + b - s0 : GT_CHUNK);
           load_chunk(a, sh, s0, cnt);
-          __syncthreads();
           accumulate_chunk(sh, cnt, R, acc, macc);
           __syncthreads();
         }
