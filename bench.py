@@ -574,7 +574,7 @@ def run_gtc(args):
     out = {}
     for name, stoch, it in [("stochastic", True, args.gtc_epochs), ("full", False, args.gtc_full_iters)]:
         o = pkg.SparseOptions(order=3, rank=R, tnsDims=dims, max_iter=it, lambdas=[1e-3] * 3,
-                              c_stochastic_perc=0.01, factorsInit=init, threshold_error=0.0)
+                              c_stochastic_perc=args.gtc_c, factorsInit=init, threshold_error=0.0)
         pkg.gtc_device(idx_tr.data_ptr(), vals_tr.data_ptr(), n_train,
                        dataclasses_replace(o, max_iter=1), stochastic=stoch, ctx=ctx)   # warm-up
         torch.cuda.synchronize()
@@ -587,11 +587,12 @@ def run_gtc(args):
                      "observed_entries_per_s": n_train * max(1, passes) / el,
                      "rel_cost": st.rel_costFunction, "heldout_rmse": rmse(st.factors)}
     floor = float(torch.sqrt(torch.mean((clean_ho - vals_ho) ** 2)))
-    line = {"metric": "observed entries/s, stochastic GTC 50000x50000x5000, 200M entries, R=32, c=0.01",
+    line = {"metric": f"observed entries/s, stochastic GTC 50000x50000x5000, {total_nnz / 1e6:g}M entries, R=32, "
+                      f"c={args.gtc_c:g}",
             "value": out["stochastic"]["observed_entries_per_s"], "unit": "entries/s", "n_gpus": 1,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic (uniform sample, rank-32 model, 10% noise)",
             "config": {"workload": "gtc_stochastic 50000x50000x5000", "nnz_train": n_train, "nnz_heldout": n_hold,
-                       "rank": R, "lambda": 1e-3, "c_stochastic_perc": 0.01},
+                       "rank": R, "lambda": 1e-3, "c_stochastic_perc": args.gtc_c},
             "runs": out, "heldout_rmse_noise_floor": floor}
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -623,6 +624,7 @@ def main():
     ap.add_argument("--gtc-nnz", type=float, default=200e6)
     ap.add_argument("--gtc-epochs", type=int, default=2, help="stochastic GTC epochs (its max_iter)")
     ap.add_argument("--gtc-full-iters", type=int, default=2)
+    ap.add_argument("--gtc-c", type=float, default=0.01, help="sampled fraction of each row per inner step")
     ap.add_argument("--batch-sample", type=int, default=32, help="instances the CPU baseline solves")
     args = ap.parse_args()
     if args.workload == "fmri-batch":
