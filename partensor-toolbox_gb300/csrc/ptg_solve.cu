@@ -324,7 +324,9 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   float *wred = slots + 4;                          // kNnlsWarps * 2
   double *wredd = reinterpret_cast<double *>(wred + 2 * kNnlsWarps);   // kNnlsWarps
   double *ma = wredd + kNnlsWarps;                  // 1: this CTA's <M, A>
-  int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired
+  int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired, [1..3]: stop-test words
+  // RB == 1 only: the warps' Y rows, (kNnlsWarps*ROWS) x 32, on a 16-byte boundary
+  float *Ys = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(flags + 4) + 15) & ~(uintptr_t)15);
 
   const NnlsParams *np = a.np;
   const float L = (float)np->L, lam = (float)np->lambda;
@@ -452,11 +454,41 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   if (tid < 3) flags[1 + tid] = 0;
   cluster.sync();
   float g[ROWS][RB];
+  // R <= 32: this lane's column of Z~ stays in registers for the whole solve and the warp's
+  // Y rows are read back from shared memory as float4 broadcasts (4 FMAs per load) instead of
+  // one shuffle per (row, k); the FMAs and their order are the same.  Columns k >= R of Z~
+  // and of Y are zero, so the extra terms add exact zeros.
+  float zr[RB == 1 ? 32 : 1];
+  if constexpr (RB == 1) {
+#pragma unroll
+    for (int k = 0; k < 32; ++k) zr[k] = (k < R && colok[0]) ? Zt[k * R + lane] : 0.0f;
+  }
+  auto stage_y = [&]() {
+    if constexpr (RB == 1) {
+      __syncwarp();   // every lane has read the previous Y rows
+#pragma unroll
+      for (int j = 0; j < ROWS; ++j) Ys[(warp * ROWS + j) * 32 + lane] = Y[j][0];
+      __syncwarp();
+    }
+  };
   auto gradient = [&]() {   // grad = Y Z~ - W~
 #pragma unroll
     for (int j = 0; j < ROWS; ++j)
 #pragma unroll
       for (int b = 0; b < RB; ++b) g[j][b] = -Wt[j][b];
+    if constexpr (RB == 1) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+#pragma unroll
+        for (int j = 0; j < ROWS; ++j) {
+          const float4 y4 = *reinterpret_cast<const float4 *>(&Ys[(warp * ROWS + j) * 32 + 4 * q]);
+          g[j][0] = fmaf(y4.x, zr[4 * q], g[j][0]);
+          g[j][0] = fmaf(y4.y, zr[4 * q + 1], g[j][0]);
+          g[j][0] = fmaf(y4.z, zr[4 * q + 2], g[j][0]);
+          g[j][0] = fmaf(y4.w, zr[4 * q + 3], g[j][0]);
+        }
+      return;
+    }
     for (int k = 0; k < R; ++k) {
       const int kb = k >> 5, kl = k & 31;
       float z[RB];
@@ -470,6 +502,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
       }
     }
   };
+  stage_y();
   gradient();
   int it = 0;
   for (;;) {
@@ -495,6 +528,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
         Ac[j][b] = na;
       }
     asm volatile("barrier.cluster.arrive.release;" ::: "memory");
+    stage_y();
     gradient();   // of it+1 (discarded if it stops at it)
     asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
     if (*(volatile int *)&vflag0[it % 3] == 0) {   // no violation: stop, the result is A_it
@@ -615,7 +649,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
 template <int RB, int ROWS>
 size_t nnls_smem_bytes(int R) {
   return sizeof(float) * (2 * R * R + kNnlsWarps * ROWS * R + ((R + 1) & ~1) + 4 + 2 * kNnlsWarps) +
-         sizeof(double) * (kNnlsWarps + 2) + 16;
+         sizeof(double) * (kNnlsWarps + 2) + 16 + (RB == 1 ? 16 + sizeof(float) * kNnlsWarps * ROWS * 32 : 0);
 }
 
 template <int RB, int ROWS>
