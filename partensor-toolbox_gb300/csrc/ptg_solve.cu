@@ -324,9 +324,13 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   float *wred = slots + 4;                          // kNnlsWarps * 2
   double *wredd = reinterpret_cast<double *>(wred + 2 * kNnlsWarps);   // kNnlsWarps
   double *ma = wredd + kNnlsWarps;                  // 1: this CTA's <M, A>
-  int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired, [1..3]: stop-test words
+  int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired, [1..3]: stop-test words (CTA 0's
+                                                    // are the cluster's), [4..7]: unused
+  float *bt = reinterpret_cast<float *>(flags + 8); // kMaxInner: the beta sequence
+  float *rsc = bt + kMaxInner;                      // kNnlsWarps*ROWS: row scales of the warm start
   // RB == 1 only: the warps' Y rows, (kNnlsWarps*ROWS) x 32, on a 16-byte boundary
-  float *Ys = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(flags + 4) + 15) & ~(uintptr_t)15);
+  float *Ys = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(rsc + kNnlsWarps * ROWS) + 15) &
+                                        ~(uintptr_t)15);
 
   const NnlsParams *np = a.np;
   const float L = (float)np->L, lam = (float)np->lambda;
@@ -336,6 +340,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
     if (idx / R == idx % R) z += lam;               // Z~ = Z + lambda I   (:205)
     Zt[idx] = z;
   }
+  for (int k = tid; k < kMaxInner; k += blockDim.x) bt[k] = np->beta[k];
 
   // rows of this lane: row(j) = gw + j * (CS * warps)
   const int gw = rank * kNnlsWarps + warp;
@@ -361,7 +366,6 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
     }
   }
   // ---- learned warm start: features of each row, network inference, logging ----
-  float rscale[ROWS];
   if (a.theta || a.log_X) {
     const int Din = R + 8, H = a.hidden;
     const float Lf = (float)np->L;
@@ -381,7 +385,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
       }
       for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
       const float sc = sqrtf(s2) + 1e-30f;
-      rscale[j] = sc;
+      if (lane == 0) rsc[warp * ROWS + j] = sc;
       float x[RB];
 #pragma unroll
       for (int b = 0; b < RB; ++b) x[b] = m[b] / sc;
@@ -517,7 +521,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
     }
     if (__any_sync(0xffffffffu, viol) && lane == 0) *(volatile int *)&vflag0[it % 3] = 1;
     if (rank == 0 && tid == 0) flags[1 + (it + 1) % 3] = 0;   // the word of it+1 (read last at it-2)
-    const float beta = np->beta[it];
+    const float beta = bt[it];
 #pragma unroll
     for (int j = 0; j < ROWS; ++j)
 #pragma unroll
@@ -600,7 +604,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
       if (i < I && colok[b]) {
         const float v = As[(warp * ROWS + j) * R + c];
         a.A[(size_t)i * R + c] = v;
-        if (a.log_T) a.log_T[(size_t)i * R + c] = v * (float)np->L / rscale[j];
+        if (a.log_T) a.log_T[(size_t)i * R + c] = v * (float)np->L / rsc[warp * ROWS + j];
       }
     }
   }
@@ -649,7 +653,8 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
 template <int RB, int ROWS>
 size_t nnls_smem_bytes(int R) {
   return sizeof(float) * (2 * R * R + kNnlsWarps * ROWS * R + ((R + 1) & ~1) + 4 + 2 * kNnlsWarps) +
-         sizeof(double) * (kNnlsWarps + 2) + 16 + (RB == 1 ? 16 + sizeof(float) * kNnlsWarps * ROWS * 32 : 0);
+         sizeof(double) * (kNnlsWarps + 2) + 32 + sizeof(float) * (kMaxInner + kNnlsWarps * ROWS) +
+         (RB == 1 ? 16 + sizeof(float) * kNnlsWarps * ROWS * 32 : 0);
 }
 
 template <int RB, int ROWS>
