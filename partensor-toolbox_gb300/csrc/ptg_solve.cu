@@ -324,8 +324,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   float *wred = slots + 4;                          // kNnlsWarps * 2
   double *wredd = reinterpret_cast<double *>(wred + 2 * kNnlsWarps);   // kNnlsWarps
   double *ma = wredd + kNnlsWarps;                  // 1: this CTA's <M, A>
-  int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired, [1..3]: stop-test words (CTA 0's
-                                                    // are the cluster's), [4..7]: unused
+  int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired, [1..3]: stop-test words, [4..7]: unused
   float *bt = reinterpret_cast<float *>(flags + 8); // kMaxInner: the beta sequence
   float *rsc = bt + kMaxInner;                      // kNnlsWarps*ROWS: row scales of the warm start
   // RB == 1 only: the warps' Y rows, (kNnlsWarps*ROWS) x 32, on a 16-byte boundary
@@ -453,7 +452,8 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   // shared memory (three words used in rotation).  One split cluster barrier per iteration:
   // arrive after the flag write and the speculative update, wait after the next gradient, so
   // the barrier's latency hides behind that product.  The update of iteration `it` keeps A_it
-  // in the staging rows (As) in case the flag says stop.
+  // in the staging rows (As) in case the flag says stop.  (Copies of the words in every CTA,
+  // written by lanes 0..CS-1 of a violating warp and read locally, measured no faster.)
   int *vflag0 = cluster.map_shared_rank(flags + 1, 0);
   if (tid < 3) flags[1 + tid] = 0;
   cluster.sync();
@@ -491,18 +491,18 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
           g[j][0] = fmaf(y4.z, zr[4 * q + 2], g[j][0]);
           g[j][0] = fmaf(y4.w, zr[4 * q + 3], g[j][0]);
         }
-      return;
-    }
-    for (int k = 0; k < R; ++k) {
-      const int kb = k >> 5, kl = k & 31;
-      float z[RB];
+    } else {
+      for (int k = 0; k < R; ++k) {
+        const int kb = k >> 5, kl = k & 31;
+        float z[RB];
 #pragma unroll
-      for (int b = 0; b < RB; ++b) z[b] = colok[b] ? Zt[k * R + lane + 32 * b] : 0.f;
+        for (int b = 0; b < RB; ++b) z[b] = colok[b] ? Zt[k * R + lane + 32 * b] : 0.f;
 #pragma unroll
-      for (int j = 0; j < ROWS; ++j) {
-        const float yk = __shfl_sync(0xffffffffu, kb == 0 ? Y[j][0] : Y[j][RB - 1], kl);
+        for (int j = 0; j < ROWS; ++j) {
+          const float yk = __shfl_sync(0xffffffffu, kb == 0 ? Y[j][0] : Y[j][RB - 1], kl);
 #pragma unroll
-        for (int b = 0; b < RB; ++b) g[j][b] = fmaf(yk, z[b], g[j][b]);
+          for (int b = 0; b < RB; ++b) g[j][b] = fmaf(yk, z[b], g[j][b]);
+        }
       }
     }
   };
