@@ -96,6 +96,23 @@ struct ptg_tensor {
 
 namespace ptg {
 
+// Sum of nsplit split-K partials p[0], p[step], p[2 step], ... in split order.  Loads go out
+// eight at a time so that their latencies overlap; the additions keep the split order, so
+// the result does not depend on the batching.
+__device__ __forceinline__ float sum_splits(const float *__restrict__ p, int64_t step, int nsplit) {
+  float s = 0.0f;
+  int sp = 0;
+  for (; sp + 8 <= nsplit; sp += 8) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldg(p + (int64_t)(sp + u) * step);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s += v[u];
+  }
+  for (; sp < nsplit; ++sp) s += __ldg(p + (int64_t)sp * step);
+  return s;
+}
+
 // Description of one MTTKRP-shaped contraction over the tensor viewed as [P, Q, S]:
 //   out[q, r] = sum_{p, s} X[p + P*q + P*Q*s] * KRb[p, r] * KRa[s, r]
 // KRb is the Khatri-Rao row of the factors of the modes before q (digits of p, fastest

@@ -332,9 +332,7 @@ __global__ void splitk_reduce_kernel(const float *__restrict__ partial, int nspl
     const int64_t q = idx / BN;
     const int c = (int)(idx % BN);
     if (col0 + c >= R) continue;
-    float s = 0.0f;
-    for (int sp = 0; sp < nsplit; ++sp) s += partial[((int64_t)sp * Q + q) * BN + c];
-    out[q * ldo + col0 + c] = s;
+    out[q * ldo + col0 + c] = sum_splits(partial + q * BN + c, Q * BN, nsplit);
   }
 }
 

@@ -388,9 +388,7 @@ __global__ void tc32_reduce_kernel(const float *__restrict__ partial, int nsplit
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t q = idx / R;
     const int c = (int)(idx % R);
-    float s = 0.0f;
-    for (int sp = 0; sp < nsplit; ++sp) s += partial[((int64_t)sp * Q + q) * N + c];
-    out[idx] = s;
+    out[idx] = sum_splits(partial + q * N + c, Q * N, nsplit);
   }
 }
 
