@@ -719,7 +719,18 @@ __global__ void gram_partial_kernel(const float *__restrict__ A, int I, int R,
   extern __shared__ float rows[];   // kGramRowsPerBlock x R
   const int r0 = blockIdx.x * kGramRowsPerBlock;
   const int nr = min(kGramRowsPerBlock, I - r0);
-  for (int idx = threadIdx.x; idx < nr * R; idx += blockDim.x) rows[idx] = A[(size_t)r0 * R + idx];
+  // stage the block's rows: eight independent loads in flight per thread, not one
+  const float *src = A + (size_t)r0 * R;
+  const int n = nr * R, step = blockDim.x;
+  int idx0 = threadIdx.x;
+  for (; idx0 + 7 * step < n; idx0 += 8 * step) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldg(src + idx0 + u * step);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) rows[idx0 + u * step] = v[u];
+  }
+  for (; idx0 < n; idx0 += step) rows[idx0] = __ldg(src + idx0);
   __syncthreads();
   for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
     const int a = idx / R, b = idx % R;
