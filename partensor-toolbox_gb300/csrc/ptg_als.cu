@@ -120,7 +120,9 @@ struct Runner {
       }
       PTG_CUDA(cudaEventRecord(ctx->ev_fork, S));
       PTG_CUDA(cudaStreamWaitEvent(T, ctx->ev_fork, 0));
-      PTG_TRY(launch_eigen_bounds(b.gram, N, n, R, b.np, T));
+      // beside the tensor-core MTTKRP: a direct contraction, or the node contraction of a tree
+      const bool beside_tc = contraction_uses_tc(ctx, X, R) && (!dimtree || n == 0 || n == dimtree_split(N));
+      PTG_TRY(launch_eigen_bounds(b.gram, N, n, R, b.np, T, beside_tc));
       count_launches(ctx, 1);
       PTG_CUDA(cudaEventRecord(ctx->ev_join, T));
       if (!dimtree) {

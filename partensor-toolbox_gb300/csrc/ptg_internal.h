@@ -135,6 +135,8 @@ Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors,
 
 // Launch an MTTKRP-shaped contraction (FP32 or BF16 storage) on `stream`; out is
 // row-major [q_write][R].
+// whether contraction_launch runs this tensor's contractions on the tensor cores
+bool contraction_uses_tc(const ptg_ctx *ctx, const ptg_tensor *t, int R);
 int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                        cudaStream_t stream);
 
@@ -217,8 +219,9 @@ struct WarmArgs {
   float *log_T = nullptr;         // [rows][R] targets
 };
 
+// beside_tc: the launch runs beside a tensor-core MTTKRP and takes its shared-memory carveout
 int launch_eigen_bounds(const float *const *grams, int order, int mode, int R, NnlsParams *out,
-                        cudaStream_t stream);
+                        cudaStream_t stream, bool beside_tc = false);
 // Nesterov MNLS of one factor on a thread-block cluster; also writes the new Gram
 // (FP32 R x R), <M, A_new> and sum(Z .* G_new) in FP64, the iteration count and whether
 // the zero-column repair ran.

@@ -727,6 +727,13 @@ static double contraction_bytes(const ptg_tensor *t, const Contraction &c, int R
   return numel * esz + fac + (double)c.q_write * R * 4.0;
 }
 
+// FP32 storage reaches the tensor cores (three-term TF32 split) only on request: its
+// accumulation in TMEM carries a small negative bias that grows with the contraction length
+bool contraction_uses_tc(const ptg_ctx *ctx, const ptg_tensor *t, int R) {
+  return (t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 128) ||
+         (t->dtype == PTG_F32 && R <= 64 && ctx->mttkrp_impl == 2);
+}
+
 int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                        cudaStream_t stream) {
   if (R < 1) return set_error(PTG_ERR_INVALID, "rank must be >= 1");
@@ -737,10 +744,7 @@ int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, 
   cudaEvent_t ev = nullptr;
   PTG_TRY(stats_begin(ctx, stream, &ev));
   int rc;
-  // FP32 storage reaches the tensor cores (three-term TF32 split) only on request: its
-  // accumulation in TMEM carries a small negative bias that grows with the contraction length
-  const bool tc = (t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 128) ||
-                  (t->dtype == PTG_F32 && R <= 64 && ctx->mttkrp_impl == 2);
+  const bool tc = contraction_uses_tc(ctx, t, R);
   if (t->dtype == PTG_F32 && tc)
     rc = tc32_contraction_launch(ctx, t, c, R, out, stream);
   else if (t->dtype == PTG_F32)

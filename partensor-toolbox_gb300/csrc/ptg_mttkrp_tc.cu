@@ -368,6 +368,9 @@ int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &
   prm.err = ctx->dev_err;
   const size_t smem = tc_smem_bytes(prm.N);
   PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // the largest carveout, which the eigenvalue-bound kernel beside it asks for too
+  PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                cudaSharedmemCarveoutMaxShared));
   dim3 grid((unsigned)qgroups, (unsigned)nsplit);
   mttkrp_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(map, prm);
   PTG_CUDA(cudaGetLastError());

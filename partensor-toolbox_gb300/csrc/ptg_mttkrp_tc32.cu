@@ -484,6 +484,8 @@ int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction
   const size_t smem = tc32_smem_bytes(prm.N);
   if (smem > ctx->smem_optin) return set_error(PTG_ERR_UNSUPPORTED, "tensor-core FP32 MTTKRP: shared memory");
   PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc32_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                cudaSharedmemCarveoutMaxShared));
   dim3 grid((unsigned)qgroups, (unsigned)nsplit);
   mttkrp_tc32_kernel<<<grid, T3_THREADS, smem, stream>>>(map, prm);
   PTG_CUDA(cudaGetLastError());

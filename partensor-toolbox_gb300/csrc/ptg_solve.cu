@@ -751,10 +751,17 @@ __global__ void sum_rr_kernel(const float *__restrict__ part, int nb, int RR, fl
 }  // namespace
 
 int launch_eigen_bounds(const float *const *grams, int order, int mode, int R, NnlsParams *out,
-                        cudaStream_t stream) {
+                        cudaStream_t stream, bool beside_tc) {
   if (R > kMaxR) return set_error(PTG_ERR_UNSUPPORTED, "rank > 64 is not supported by the NNLS path");
   GramPtrs gp{};
   for (int k = 0; k < order; ++k) gp.g[k] = grams[k];
+  // CTAs of two kernels share an SM only under the same shared-memory carveout: beside the
+  // tensor-core MTTKRP (one CTA per SM, which takes the largest carveout) this kernel asks for
+  // the same, else it would wait for an SM to drain and sit on the critical path; beside the
+  // CUDA-core MTTKRP the driver's default choice is the one that fits
+  PTG_CUDA(cudaFuncSetAttribute(eigen_bounds_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                beside_tc ? (int)cudaSharedmemCarveoutMaxShared
+                                          : (int)cudaSharedmemCarveoutDefault));
   eigen_bounds_kernel<<<1, kEigThreads, 0, stream>>>(gp, order, mode, R, out);
   PTG_CUDA(cudaGetLastError());
   return PTG_OK;
