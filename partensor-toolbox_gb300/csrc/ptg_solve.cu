@@ -181,6 +181,7 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
     lohi[1][0] = lo; lohi[1][1] = hi;   // largest eigenvalue
     s_scalar[1] = fmax(fabs(lo), fabs(hi));   // ||T|| bound
   }
+  __syncthreads();   // d and e2 are complete before any thread reads them (n > 32 spans warps)
   for (int i = tid; i < n; i += blockDim.x) {
     df[i] = (float)d[i];
     e2f[i] = (float)e2[i];
