@@ -442,9 +442,10 @@ def run_batch_ours(args):
 
 
 def run_dimtree(args):
-    """160^4, R=64, collinear factors (cosine 0.6, seed 3), 25 dB: cpdDimTree to the target
-    (noise floor + 1e-3) on BF16 tcgen05 storage with the fit verified on FP32, beside the
-    plain FP32 dimension tree, the direct (non-tree) BF16 solve and the learned warm start."""
+    """160^4, R=64, collinear factors (cosine 0.6, seed 3), 25 dB: cpdDimTree in FP32 to the
+    target (noise floor + 1e-3) is the value; beside it the direct (non-tree) FP32 solve, the
+    FP32 tree with the learned warm start and the tree on BF16 tcgen05 storage with the fit
+    verified on FP32."""
     import numpy as np
     import torch
     ws, rank = _dist()

@@ -82,90 +82,108 @@ __device__ int sturm_count_f64(const double *d, const double *e2, int n, double 
 }
 
 __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R, NnlsParams *out) {
-  __shared__ double A[kMaxR * kMaxR];
-  __shared__ double v[kMaxR], p[kMaxR], w[kMaxR];
+  constexpr int lda = kMaxR + 1;              // padded rows: column reads and mirrored writes
+  __shared__ double A[kMaxR * lda];           // spread over the banks
+  __shared__ double xs[kMaxR], vs[kMaxR], ws[kMaxR];
+  __shared__ double ps[kEigThreads / kMaxR][kMaxR];
   __shared__ double d[kMaxR], e[kMaxR], e2[kMaxR];
-  __shared__ double red[kEigThreads / 32];
+  __shared__ double redb[2][kEigThreads / 32];
   __shared__ double s_scalar[4];
   __shared__ double lohi[2][2];
   __shared__ float df[kMaxR], e2f[kMaxR];
   const int tid = threadIdx.x;
   const int n = R;
 
-  // Z = prod_{k != mode} G_k (FP64), k from order-1 down to 0 as PartialCwiseProd orders it
+  // Z = prod_{k != mode} G_k (FP64), k from order-1 down to 0 as PartialCwiseProd orders it;
+  // the tridiagonalisation works on the lower triangle mirrored, so A is exactly symmetric
   for (int idx = tid; idx < n * n; idx += blockDim.x) {
+    const int i = idx / n, j = idx - (idx / n) * n;
     double z = 1.0;
     for (int k = order - 1; k >= 0; --k)
       if (k != mode) z *= (double)gp.g[k][idx];
-    A[idx] = z;
     out->Z[idx] = z;
+    if (j <= i) {
+      A[i * lda + j] = z;
+      A[j * lda + i] = z;
+    }
   }
   __syncthreads();
 
-  // Block sum: FP64 partials reduced by one thread and broadcast (GB300 executes FP64 at a
-  // small fraction of the FP32 rate, so no FP64 work is repeated across threads).
+  // Block sum: warp shuffles, then every thread adds the warps' partials in warp order from one
+  // of two alternating buffers, so a sum costs one barrier and no broadcast.  (A buffer is
+  // written again two sums later, after a barrier every thread passes once it has read it.)
+  int rb = 0;
   auto block_sum = [&](double x) -> double {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if ((tid & 31) == 0) red[tid >> 5] = x;
+    if ((tid & 31) == 0) redb[rb][tid >> 5] = x;
     __syncthreads();
-    if (tid == 0) {
-      double s = 0.0;
-      for (int i = 0; i < kEigThreads / 32; ++i) s += red[i];
-      s_scalar[2] = s;
-    }
-    __syncthreads();
-    return s_scalar[2];
+    double sum = 0.0;
+    for (int i = 0; i < kEigThreads / 32; ++i) sum += redb[rb][i];
+    rb ^= 1;
+    return sum;
   };
 
-  // ---- Householder tridiagonalisation (A symmetric, row-major n x n) ----
+  // ---- Householder tridiagonalisation (Golub & Van Loan alg. 8.3.1), H = I - beta v v^T,
+  // v = x - alpha e_1, A_sub <- A_sub - v w^T - w v^T with p = beta A_sub v, w = p - (beta/2)(p.v) v.
+  // A_sub v = A_sub x - alpha A_sub e_1: the product with x runs before alpha is known, beside
+  // the square root and the division (one thread: GB300's FP64 pipe is the scarce resource).
+  // Thread (q, i) sums a quarter of row i's terms, reading column entries (A is symmetric) so
+  // that a warp's threads read consecutive addresses. ----
+  const int pi = tid & (kMaxR - 1), pq = tid / kMaxR;
   for (int k = 0; k + 2 < n; ++k) {
-    const int m = n - k - 1;  // length of the column below the diagonal
-    // sigma = ||x[1:]||^2
-    double part = 0.0;
-    for (int i = 1 + tid; i < m; i += blockDim.x) {
-      const double xi = A[(k + 1 + i) * n + k];
-      part += xi * xi;
-    }
-    const double sigma = block_sum(part);
-    const double x0 = A[(k + 1) * n + k];
-    if (sigma == 0.0) {
+    const int m = n - k - 1;  // length of the column below the diagonal (= row k right of it)
+    const double *rowk = A + k * lda + (k + 1);
+    const double xi = tid < m ? rowk[tid] : 0.0;
+    if (tid < m) xs[tid] = xi;
+    const double sigma = block_sum(tid >= 1 && tid < m ? xi * xi : 0.0);   // ||x[1:]||^2
+    const double x0 = rowk[0];
+    if (sigma == 0.0) {   // uniform: nothing to eliminate, A unchanged
       if (tid == 0) e[k] = x0;
-      __syncthreads();
       continue;
     }
-    if (tid == 0) {   // the step's scalars, once
+    double y = 0.0;       // (A_sub x)_i, partial over j in [16 q, 16 q + 16)
+    if (pi < m) {
+      const double *col = A + (k + 1) * lda + (k + 1 + pi);
+      const int j1 = min(m, (pq + 1) * (kMaxR / (kEigThreads / kMaxR)));
+      for (int j = pq * (kMaxR / (kEigThreads / kMaxR)); j < j1; ++j) y = fma(col[j * lda], xs[j], y);
+      ps[pq][pi] = y;
+    }
+    if (tid == kEigThreads - 1) {   // never holds a row of the product (row 63 > m - 1)
       const double al = (x0 >= 0.0 ? -1.0 : 1.0) * sqrt(x0 * x0 + sigma);
+      const double dv = x0 - al;
       s_scalar[0] = al;
-      s_scalar[3] = 2.0 / ((x0 - al) * (x0 - al) + sigma);
+      s_scalar[3] = 2.0 / (dv * dv + sigma);
     }
     __syncthreads();
-    const double alpha = s_scalar[0];
-    const double beta = s_scalar[3];
-    for (int i = tid; i < m; i += blockDim.x) v[i] = (i == 0) ? (x0 - alpha) : A[(k + 1 + i) * n + k];
-    __syncthreads();
-    // p = beta * A_sub v   (rows of the trailing block split over the threads)
-    for (int i = tid; i < m; i += blockDim.x) {
-      const double *row = &A[(k + 1 + i) * n + (k + 1)];
-      double s = 0.0;
-      for (int j = 0; j < m; ++j) s = fma(row[j], v[j], s);
-      p[i] = beta * s;
+    const double alpha = s_scalar[0], beta = s_scalar[3];
+    const double v0 = x0 - alpha;
+    double pv = 0.0, vi = 0.0, pvi = 0.0;
+    if (tid < m) {
+      double yi = 0.0;
+      for (int q = 0; q < kEigThreads / kMaxR; ++q) yi += ps[q][tid];
+      vi = tid == 0 ? v0 : xi;
+      pvi = beta * fma(-alpha, A[(k + 1) * lda + (k + 1 + tid)], yi);   // p_i
+      pv = pvi * vi;
     }
-    __syncthreads();
-    part = 0.0;
-    for (int i = tid; i < m; i += blockDim.x) part = fma(p[i], v[i], part);
-    const double K = 0.5 * beta * block_sum(part);
-    for (int i = tid; i < m; i += blockDim.x) w[i] = p[i] - K * v[i];
+    const double K = 0.5 * beta * block_sum(pv);
+    if (tid < m) {
+      vs[tid] = vi;
+      ws[tid] = pvi - K * vi;
+    }
     __syncthreads();
     for (int idx = tid; idx < m * m; idx += blockDim.x) {
-      const int i = idx / m, j = idx % m;
-      A[(k + 1 + i) * n + (k + 1 + j)] -= v[i] * w[j] + w[i] * v[j];
+      const int i = idx / m, j = idx - (idx / m) * m;
+      if (j > i) continue;
+      const double a = A[(k + 1 + i) * lda + (k + 1 + j)] - (vs[i] * ws[j] + ws[i] * vs[j]);
+      A[(k + 1 + i) * lda + (k + 1 + j)] = a;
+      A[(k + 1 + j) * lda + (k + 1 + i)] = a;
     }
     if (tid == 0) e[k] = alpha;
     __syncthreads();
   }
   if (tid == 0) {
-    for (int i = 0; i < n; ++i) d[i] = A[i * n + i];
-    if (n >= 2) e[n - 2] = A[(n - 1) * n + (n - 2)];
+    for (int i = 0; i < n; ++i) d[i] = A[i * lda + i];
+    if (n >= 2) e[n - 2] = A[(n - 1) * lda + (n - 2)];
     for (int i = 0; i + 1 < n; ++i) e2[i] = e[i] * e[i];
     // Gershgorin interval
     double lo = 1e300, hi = -1e300;
