@@ -262,10 +262,13 @@ def run_ours(args):
             t = time.perf_counter()
             st_e = pkg.cpd(hnp, R, o, init, dims=dims, ctx=ctx)
             ts.append(time.perf_counter() - t)
+        # the host side is shared with other jobs on this machine: its memory and host-to-GPU
+        # link vary from call to call, so the spread of the calls is reported beside the mean
         e2e = {"value": _max_over_ranks(statistics.mean(ts), ws), "unit": "s",
                "h2d_bytes_per_step": int(hnp.nbytes + sum(f.nbytes for f in init)),
                "d2h_bytes_per_step": int(sum(f.nbytes for f in st_e.factors)),
-               "rel_err": st_e.rel_costFunction}
+               "rel_err": st_e.rel_costFunction, "min": min(ts), "median": statistics.median(ts),
+               "calls_s": [round(x, 5) for x in ts]}
         del host
 
     sweeps_plain = st_f[-1].ao_iter
@@ -611,7 +614,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--steps-plain", type=int, default=2)
-    ap.add_argument("--steps-e2e", type=int, default=2)
+    ap.add_argument("--steps-e2e", type=int, default=5)
     ap.add_argument("--max-iter", type=int, default=200)
     ap.add_argument("--small", action="store_true", help="200^3 smoke configuration")
     ap.add_argument("--dims", type=int, nargs=3, default=None, help="override the tensor shape (profiling)")
