@@ -32,8 +32,9 @@ struct AlsBuffers {
   float *TL = nullptr, *TR = nullptr;   // dimension-tree node tensors (when used)
   float *gpart = nullptr;
   NnlsParams *np = nullptr;
-  double *dsc = nullptr;  // [N][2]: <M, A>, sum(Z .* G); [N][2..3]: cost terms of a point
-  int *isc = nullptr;     // [N][2]: iterations, repaired
+  double *dsc = nullptr;  // [N][2]: <M, A>, sum(Z .* G); [0][2..3]: cost terms of a point;
+                          // [4N], [4N + 1]: the line-search decision (accel_select_kernel)
+  int *isc = nullptr;     // [N][2]: iterations, repaired; [2N]: the line search's stop gate
   double *W = nullptr;    // R x R FP64: Z^{-1} or (M^T M)^{-1/2} (other constraints)
   void *base = nullptr;
 
@@ -66,8 +67,8 @@ struct AlsBuffers {
     const size_t o_TR = take(sizeof(float) * std::max<int64_t>(rows_right, 1) * R);
     const size_t o_gp = take(sizeof(float) * gp);
     const size_t o_np = take(sizeof(NnlsParams));
-    const size_t o_d = take(sizeof(double) * 4 * N);
-    const size_t o_i = take(sizeof(int) * 2 * N);
+    const size_t o_d = take(sizeof(double) * (4 * N + 2));
+    const size_t o_i = take(sizeof(int) * (2 * N + 2));
     const size_t o_W = take(sizeof(double) * R * R);
     cudaError_t e = cudaMalloc(&base, off);
     if (e != cudaSuccess) {
@@ -97,6 +98,67 @@ struct AlsBuffers {
   }
 };
 
+// The line-search decision of include/Cpd.hpp:262-271 on the device, so that the host does not
+// wait for it: the sweep's cost and the accelerated point's cost from their terms (the host's
+// arithmetic in the host's order: the doublings are exact, so contraction cannot change a
+// result), the stop test of the sweep, then acc -> fac and gacc -> gram when the point is
+// taken.  Every block decides alike; block 0 records the point's f^2 and the decision.
+struct SelectArgs {
+  const double *dsc;     // sweep terms at [4 last], [4 last + 1]; the point's at [2], [3]
+  int last, N, R;
+  double frob, threshold;
+  int ao_iter, max_iter;
+  int rows[PTG_MAX_ORDER];
+  float *fac[PTG_MAX_ORDER];
+  float *gram[PTG_MAX_ORDER];
+  const float *acc[PTG_MAX_ORDER];
+  const float *gacc[PTG_MAX_ORDER];
+  double *sel;           // out: [0] the point's f^2, [1] 1.0 when taken
+};
+
+__global__ void accel_select_kernel(const SelectArgs a) {
+  __shared__ int take;
+  if (threadIdx.x == 0) {
+    const double f2 = a.frob - 2.0 * a.dsc[4 * a.last] + a.dsc[4 * a.last + 1];
+    const double fa2 = a.frob + a.dsc[3] - 2.0 * a.dsc[2];
+    const double f = sqrt(fmax(f2, 0.0)), fa = sqrt(fmax(fa2, 0.0));
+    const bool stop = f / sqrt(a.frob) < a.threshold || a.ao_iter >= a.max_iter;
+    take = (!stop && f > fa) ? 1 : 0;   // a NaN cost compares false: nothing is taken
+    if (blockIdx.x == 0) {
+      a.sel[0] = fa2;
+      a.sel[1] = take ? 1.0 : 0.0;
+    }
+  }
+  __syncthreads();
+  if (!take) return;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int k = 0; k < a.N; ++k) {
+    const int64_t n = (int64_t)a.rows[k] * a.R;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) a.fac[k][i] = a.acc[k][i];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)a.R * a.R; i += stride)
+      a.gram[k][i] = a.gacc[k][i];
+  }
+}
+
+// The stop test of the sweep just queued, for the line search queued behind it: that line
+// search's MTTKRP returns at once when the sweep is the last (Contraction::skip), so a stopping
+// sweep does not pay for it.  Same arithmetic as accel_select_kernel and the host.
+__global__ void stop_gate_kernel(const double *dsc, int last, double frob, double threshold, int ao_iter,
+                                 int max_iter, int *gate) {
+  const double f2 = frob - 2.0 * dsc[4 * last] + dsc[4 * last + 1];
+  const double f = sqrt(fmax(f2, 0.0));
+  *gate = (f / sqrt(frob) < threshold || ao_iter >= max_iter) ? 1 : 0;
+}
+
+// page-locked copy of the per-sweep scalars (ptg_ctx::pinned_scalars)
+struct HostScalars {
+  double dsc[4 * PTG_MAX_ORDER];
+  int isc[2 * PTG_MAX_ORDER];
+  int err, pad;
+  double sel[2];   // the line search: the point's f^2, taken (1.0) or not
+};
+static_assert(sizeof(HostScalars) <= kPinnedScalarBytes, "pinned scalar block too small");
+
 struct Runner {
   ptg_ctx *ctx;
   const ptg_cpd_options *opt;
@@ -107,9 +169,18 @@ struct Runner {
   WarmArgs warm[PTG_MAX_ORDER];   // per mode, for the sweep being run
   std::chrono::steady_clock::time_point t0;
 
-  // one ALS sweep over all modes on tensor X; fills f (before acceleration) and per-mode
-  // iteration counts
+  HostScalars *hs() const { return static_cast<HostScalars *>(ctx->pinned_scalars); }
+
+  // one ALS sweep over all modes on tensor X, then sweep_finish: f (before acceleration) and
+  // the per-mode iteration counts
   int sweep(const ptg_tensor *X, double frob, double *f_out, int *iters) {
+    PTG_TRY(sweep_enqueue(X));
+    return sweep_finish(frob, f_out, iters);
+  }
+
+  // the sweep's kernels, then its cost terms, iteration counts and the device error word
+  // copied to pinned memory behind them (ctx->ev_cost); nothing waits
+  int sweep_enqueue(const ptg_tensor *X) {
     cudaStream_t S = ctx->stream, T = ctx->side;
     const int N = b.N, R = b.R;
     for (int n = 0; n < N; ++n) {
@@ -142,16 +213,70 @@ struct Runner {
                                b.dsc + 4 * n + 1, b.isc + 2 * n, b.isc + 2 * n + 1, S, warm[n]));
       count_launches(ctx, 1);
     }
-    double hd[4 * PTG_MAX_ORDER];
-    int hi[2 * PTG_MAX_ORDER];
-    PTG_CUDA(cudaMemcpyAsync(hd, b.dsc, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, S));
-    PTG_CUDA(cudaMemcpyAsync(hi, b.isc, sizeof(int) * 2 * N, cudaMemcpyDeviceToHost, S));
-    PTG_TRY(check_device_error(ctx));
-    const int last = N - 1;
-    const double f2 = frob - 2.0 * hd[4 * last] + hd[4 * last + 1];
+    HostScalars *h = hs();
+    PTG_CUDA(cudaMemcpyAsync(h->dsc, b.dsc, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, S));
+    PTG_CUDA(cudaMemcpyAsync(h->isc, b.isc, sizeof(int) * 2 * N, cudaMemcpyDeviceToHost, S));
+    PTG_CUDA(cudaMemcpyAsync(&h->err, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, S));
+    PTG_CUDA(cudaEventRecord(ctx->ev_cost, S));
+    return PTG_OK;
+  }
+
+  // waits for the scalars of the last queued sweep
+  int sweep_finish(double frob, double *f_out, int *iters) {
+    PTG_CUDA(cudaEventSynchronize(ctx->ev_cost));
+    const HostScalars *h = hs();
+    PTG_TRY(report_device_error(ctx, h->err));
+    const int N = b.N, last = N - 1;
+    const double f2 = frob - 2.0 * h->dsc[4 * last] + h->dsc[4 * last + 1];
     if (!std::isfinite(f2)) return set_error(PTG_ERR_NUMERIC, "cost is NaN or Inf");
     *f_out = std::sqrt(std::max(f2, 0.0));
-    for (int n = 0; n < N; ++n) iters[n] = hi[2 * n];
+    for (int n = 0; n < N; ++n) iters[n] = h->isc[2 * n];
+    return PTG_OK;
+  }
+
+  // the line-search point's cost terms (one last-mode MTTKRP in the Gram form) into
+  // b.dsc[2..3], queued
+  int point_cost_enqueue(const ptg_tensor *X, float *const *factors, float *const *grams,
+                         const int *skip = nullptr) {
+    cudaStream_t S = ctx->stream;
+    const int last = b.N - 1;
+    Contraction c = mttkrp_contraction(X, factors, last);
+    c.skip = skip;
+    PTG_TRY(contraction_launch(ctx, X, c, b.R, b.M, S));
+    PTG_TRY(launch_cost_terms(b.M, factors[last], b.rows[last], grams, b.N, b.R, b.dsc + 2, S));
+    count_launches(ctx, 1);
+    return PTG_OK;
+  }
+
+  // accel_select_kernel behind the point's cost, its decision copied to pinned memory
+  // (ctx->ev_sel)
+  int select_enqueue(double frob, double threshold, int ao_iter, int max_iter) {
+    cudaStream_t S = ctx->stream;
+    SelectArgs a{};
+    a.dsc = b.dsc;
+    a.N = b.N;
+    a.R = b.R;
+    a.last = b.N - 1;
+    a.frob = frob;
+    a.threshold = threshold;
+    a.ao_iter = ao_iter;
+    a.max_iter = max_iter;
+    int64_t most = 0;
+    for (int k = 0; k < b.N; ++k) {
+      a.rows[k] = b.rows[k];
+      a.fac[k] = b.fac[k];
+      a.gram[k] = b.gram[k];
+      a.acc[k] = b.acc[k];
+      a.gacc[k] = b.gacc[k];
+      most = std::max<int64_t>(most, (int64_t)b.rows[k] * b.R);
+    }
+    a.sel = b.dsc + 4 * b.N;
+    const int blocks = (int)std::min<int64_t>((most + 255) / 256, (int64_t)ctx->sm_count);
+    accel_select_kernel<<<std::max(blocks, 1), 256, 0, S>>>(a);
+    PTG_CUDA(cudaGetLastError());
+    count_launches(ctx, 1);
+    PTG_CUDA(cudaMemcpyAsync(hs()->sel, a.sel, sizeof(double) * 2, cudaMemcpyDeviceToHost, S));
+    PTG_CUDA(cudaEventRecord(ctx->ev_sel, S));
     return PTG_OK;
   }
 
@@ -198,11 +323,7 @@ struct Runner {
   int point_cost(const ptg_tensor *X, double frob, float *const *factors, float *const *grams,
                  double *f_out) {
     cudaStream_t S = ctx->stream;
-    const int last = b.N - 1;
-    Contraction c = mttkrp_contraction(X, factors, last);
-    PTG_TRY(contraction_launch(ctx, X, c, b.R, b.M, S));
-    PTG_TRY(launch_cost_terms(b.M, factors[last], b.rows[last], grams, b.N, b.R, b.dsc + 2, S));
-    count_launches(ctx, 1);
+    PTG_TRY(point_cost_enqueue(X, factors, grams));
     double h[2];
     PTG_CUDA(cudaMemcpyAsync(h, b.dsc + 2, sizeof(h), cudaMemcpyDeviceToHost, S));
     PTG_TRY(check_device_error(ctx));
@@ -323,6 +444,26 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
     logT = logX + rows * (rank + 8);
   }
   int64_t logged = 0;
+  bool sel_pending = false;   // a line search is queued and its decision not yet read
+  int sel_sweep = 0;          // the trace entry of that sweep
+  // a queued line search's outcome: its sweep's trace entry and the acceleration bookkeeping
+  // (include/Cpd.hpp:270-277)
+  auto take_selection = [&](int sweep_index) -> int {
+    PTG_CUDA(cudaEventSynchronize(ctx->ev_sel));
+    const double fa2 = run.hs()->sel[0];
+    if (!std::isfinite(fa2)) return set_error(PTG_ERR_NUMERIC, "cost is NaN or Inf");
+    const bool taken = run.hs()->sel[1] != 0.0;
+    if (trace) {
+      trace[sweep_index].f_accel = std::sqrt(std::max(fa2, 0.0));
+      trace[sweep_index].accel_accepted = taken ? 1 : 0;
+    }
+    if (!taken) opt.accel_fail++;
+    if (opt.accel_fail == 5) {
+      opt.accel_fail = 0;
+      opt.accel_coeff++;
+    }
+    return PTG_OK;
+  };
   for (;;) {
     ++ao_iter;
     for (int n = 0; n < N; ++n) run.warm[n] = WarmArgs();
@@ -343,23 +484,24 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
         }
       }
     }
-    PTG_TRY(run.sweep(Xa, frob, &f, iters));
+    // The sweep, its normalisation and its line search are queued before the host waits for
+    // the sweep's cost: the line search's accept decision and the stop test gating it run on
+    // the device (accel_select_kernel), and the host reads the decision one sweep later, before
+    // the next line search needs it.  The stream never idles on a host round trip.
+    PTG_TRY(run.sweep_enqueue(Xa));
     if (model && ao_iter == log_sweeps && opt.warm_train_steps > 0) {
       double loss = 0.0;
       PTG_TRY(ptg_mlp_train(ctx, model, logX, logT, logged, opt.warm_train_steps, 256, 1e-3f, 1234, &loss));
     }
-    for (int n = 0; n < N; ++n) inner_total += iters[n];
-    rel = f / std::sqrt(frob);
     if (opt.normalization && !run.all_orth) {
       PTG_TRY(launch_normalize(b.fac, b.gram, b.rows, N, run.weight, rank, S));
       count_launches(ctx, 2);
     }
-    ptg_sweep_trace tr{};
-    tr.f_value = f;
-    tr.rel_costFunction = rel;
-    for (int n = 0; n < N; ++n) tr.nesterov_iters[n] = iters[n];
-    const bool stop = rel < opt.threshold_error || ao_iter >= opt.max_iter;
-    if (!stop && opt.acceleration) {
+    if (sel_pending) {   // the previous sweep's line search (include/Cpd.hpp:247-278)
+      PTG_TRY(take_selection(sel_sweep));
+      sel_pending = false;
+    }
+    if (opt.acceleration && ao_iter < opt.max_iter) {   // at max_iter the sweep stops anyway
       if (ao_iter > 1) {
         const double step = std::pow((double)(ao_iter + 1), 1.0 / (double)opt.accel_coeff);
         PTG_TRY(launch_accel_combine(b.fac, b.old, b.acc, b.rows, N, rank, step, S));
@@ -368,33 +510,38 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
         for (int k = 0; k < N; ++k)
           PTG_CUDA(cudaMemcpyAsync(b.old[k], b.fac[k], sizeof(float) * b.rows[k] * rank,
                                    cudaMemcpyDeviceToDevice, S));
-        double fa = 0.0;
-        PTG_TRY(run.point_cost(Xa, frob, b.acc, b.gacc, &fa));
-        tr.f_accel = fa;
-        if (f > fa) {
-          for (int k = 0; k < N; ++k) {
-            std::swap(b.fac[k], b.acc[k]);
-            std::swap(b.gram[k], b.gacc[k]);
-          }
-          f = fa;
-          tr.accel_accepted = 1;
-        } else {
-          opt.accel_fail++;
-        }
-        if (opt.accel_fail == 5) {
-          opt.accel_fail = 0;
-          opt.accel_coeff++;
-        }
+        int *gate = b.isc + 2 * N;
+        stop_gate_kernel<<<1, 1, 0, S>>>(b.dsc, N - 1, frob, opt.threshold_error, ao_iter, opt.max_iter, gate);
+        PTG_CUDA(cudaGetLastError());
+        count_launches(ctx, 1);
+        PTG_TRY(run.point_cost_enqueue(Xa, b.acc, b.gacc, gate));
+        PTG_TRY(run.select_enqueue(frob, opt.threshold_error, ao_iter, opt.max_iter));
+        sel_pending = true;
+        sel_sweep = ntrace;
       } else {
         for (int k = 0; k < N; ++k)
           PTG_CUDA(cudaMemcpyAsync(b.old[k], b.fac[k], sizeof(float) * b.rows[k] * rank,
                                    cudaMemcpyDeviceToDevice, S));
       }
     }
+    PTG_TRY(run.sweep_finish(frob, &f, iters));
+    for (int n = 0; n < N; ++n) inner_total += iters[n];
+    rel = f / std::sqrt(frob);
+    ptg_sweep_trace tr{};
+    tr.f_value = f;
+    tr.rel_costFunction = rel;
+    for (int n = 0; n < N; ++n) tr.nesterov_iters[n] = iters[n];
+    const bool stop = rel < opt.threshold_error || ao_iter >= opt.max_iter;
     tr.seconds = run.elapsed();
     if (trace) trace[ntrace] = tr;
     ++ntrace;
     if (stop) break;
+  }
+  if (sel_pending) {
+    // queued behind the stopping sweep: the device's stop test gated it, nothing was taken
+    PTG_CUDA(cudaEventSynchronize(ctx->ev_sel));
+    if (run.hs()->sel[1] != 0.0) return set_error(PTG_ERR_CUDA, "internal: line search taken after the stop");
+    sel_pending = false;
   }
   // FP32 refinement sweeps on the FP32 copy (no acceleration)
   int refined = 0;

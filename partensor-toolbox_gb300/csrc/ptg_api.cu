@@ -99,6 +99,10 @@ int check_device_error(ptg_ctx *ctx) {
   int h = 0;
   PTG_CUDA(cudaMemcpyAsync(&h, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   PTG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return report_device_error(ctx, h);
+}
+
+int report_device_error(ptg_ctx *ctx, int h) {
   if (h != 0) {
     PTG_CUDA(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
     PTG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -231,6 +235,9 @@ int ptg_ctx_create(int device, ptg_ctx **out) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_cost, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_sel, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaHostAlloc(&c->pinned_scalars, kPinnedScalarBytes, cudaHostAllocDefault);
   if (e == cudaSuccess) e = cudaMalloc(&c->dev_err, 256);
   if (e == cudaSuccess) e = cudaMemset(c->dev_err, 0, 256);
   if (e != cudaSuccess) {
@@ -255,6 +262,9 @@ int ptg_ctx_destroy(ptg_ctx *c) {
   c->cache_xr.release();
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_cost) cudaEventDestroy(c->ev_cost);
+  if (c->ev_sel) cudaEventDestroy(c->ev_sel);
+  if (c->pinned_scalars) cudaFreeHost(c->pinned_scalars);
   if (c->side) cudaStreamDestroy(c->side);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;

@@ -79,6 +79,10 @@ struct ptg_ctx {
   ptg::DevBuf cache_x, cache_xr;
   void *pinned = nullptr;             // page-locked host staging, kept between calls
   size_t pinned_bytes = 0;
+  // the ALS loop's per-sweep scalars, read back without stalling the stream
+  void *pinned_scalars = nullptr;     // kPinnedScalarBytes, page-locked
+  cudaEvent_t ev_cost = nullptr;      // a sweep's cost terms have landed in pinned_scalars
+  cudaEvent_t ev_sel = nullptr;       // a line-search decision has landed in pinned_scalars
 };
 
 struct ptg_tensor {
@@ -128,15 +132,18 @@ struct Contraction {
   int64_t P = 1, Q = 1, S = 1;
   KrSide before, after;
   int64_t q_write = 0;  // rows of `out` written (q < q_write)
+  const int *skip = nullptr;   // device word: when nonzero at launch time the kernels do nothing
 };
 
 // Build the contraction of a mode-n MTTKRP of tensor t.
 Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors, int mode);
 
-// Launch an MTTKRP-shaped contraction (FP32 or BF16 storage) on `stream`; out is
-// row-major [q_write][R].
+constexpr size_t kPinnedScalarBytes = 4096;
+
 // whether contraction_launch runs this tensor's contractions on the tensor cores
 bool contraction_uses_tc(const ptg_ctx *ctx, const ptg_tensor *t, int R);
+// Launch an MTTKRP-shaped contraction (FP32 or BF16 storage) on `stream`; out is
+// row-major [q_write][R].
 int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                        cudaStream_t stream);
 
@@ -166,6 +173,9 @@ int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction
                             cudaStream_t stream);
 // Reads and clears the device error word (synchronises the stream first).
 int check_device_error(ptg_ctx *ctx);
+// the error word's value h, read back by the caller after the stream reached it: resets the
+// word and reports h (PTG_OK when 0)
+int report_device_error(ptg_ctx *ctx, int h);
 
 // A batch of MTTKRP-shaped contractions (one per instance, same layout class, FP32
 // storage) planned once into a device work list of (member, m-tile, K-split) items; all

@@ -37,6 +37,7 @@ struct SimtParams {
   int64_t q_write;
   int ldo;
   int nsplit;
+  const int *skip;   // nonzero: return at once (Contraction::skip; single launches only)
 };
 
 template <typename T>
@@ -319,13 +320,15 @@ __device__ __forceinline__ void mttkrp_simt_body(const SimtParams &prm, int mtil
 
 template <typename T, int BN, bool MMAJOR>
 __global__ void __launch_bounds__(kThreads) mttkrp_simt_kernel(const SimtParams prm) {
+  if (prm.skip && *prm.skip) return;
   mttkrp_simt_body<T, BN, MMAJOR>(prm, blockIdx.x, blockIdx.y);
 }
 
 // out[q, col0 + c] = sum over splits of partial[split][q][c], in split order.
 __global__ void splitk_reduce_kernel(const float *__restrict__ partial, int nsplit, int64_t Q,
                                      int BN, int64_t q_write, int R, int col0, int ldo,
-                                     float *__restrict__ out) {
+                                     float *__restrict__ out, const int *skip) {
+  if (skip && *skip) return;
   const int64_t n = q_write * BN;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -361,6 +364,7 @@ int launch_cfg(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, i
   using Cf = Cfg<BN>;
   const bool mmajor = (c.P == 1);
   SimtParams prm{};
+  prm.skip = c.skip;
   prm.X = t->data;
   prm.P = c.P;
   prm.Q = c.Q;
@@ -408,7 +412,7 @@ int launch_cfg(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, i
     const int64_t n = c.q_write * BN;
     const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->sm_count * 8);
     splitk_reduce_kernel<<<std::max(blocks, 1), 256, 0, stream>>>(
-        prm.partial, (int)nsplit, c.Q, BN, c.q_write, R, col0, R, out);
+        prm.partial, (int)nsplit, c.Q, BN, c.q_write, R, col0, R, out, c.skip);
     PTG_CUDA(cudaGetLastError());
   }
   return PTG_OK;
@@ -439,6 +443,7 @@ int launch_cfg_fixed(const ptg_tensor *t, const Contraction &c, int R, int col0,
   using Cf = Cfg<BN>;
   const bool mmajor = (c.P == 1);
   SimtParams prm{};
+  prm.skip = c.skip;
   prm.X = t->data;
   prm.P = c.P;
   prm.Q = c.Q;
@@ -486,7 +491,7 @@ int launch_cfg_fixed(const ptg_tensor *t, const Contraction &c, int R, int col0,
   const int64_t n = c.q_write * BN;
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)sm_count * 8);
   splitk_reduce_kernel<<<std::max(blocks, 1), 256, 0, stream>>>(scratch, (int)nsplit, c.Q, BN, c.q_write, R,
-                                                                col0, R, out);
+                                                                col0, R, out, c.skip);
   PTG_CUDA(cudaGetLastError());
   return PTG_OK;
 }

@@ -43,10 +43,12 @@ struct TcParams {
   KrDevTc before, after;
   float *partial;  // [nsplit][Q][N]
   int *err;
+  const int *skip;  // nonzero: return at once (Contraction::skip)
 };
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
 mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
+  if (prm.skip && *prm.skip) return;   // before any barrier or TMEM allocation
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   // 1024-byte aligned carve: A ring, K ring, barriers
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -267,7 +269,8 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
 }
 
 __global__ void tc_reduce_kernel(const float *__restrict__ partial, int nsplit, int64_t Q, int N, int64_t q_write,
-                                 int R, float *__restrict__ out) {
+                                 int R, float *__restrict__ out, const int *skip) {
+  if (skip && *skip) return;
   const int64_t n = q_write * R;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -366,6 +369,7 @@ int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &
   PTG_TRY(ctx->scratch.ensure(part_bytes));
   prm.partial = reinterpret_cast<float *>(ctx->scratch.ptr);
   prm.err = ctx->dev_err;
+  prm.skip = c.skip;
   const size_t smem = tc_smem_bytes(prm.N);
   PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // the largest carveout, which the eigenvalue-bound kernel beside it asks for too
@@ -377,7 +381,7 @@ int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &
   const int64_t n = c.q_write * R;
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->sm_count * 8);
   tc_reduce_kernel<<<std::max(blocks, 1), 256, 0, stream>>>(prm.partial, (int)nsplit, c.Q, prm.N, c.q_write, R,
-                                                            out);
+                                                            out, c.skip);
   PTG_CUDA(cudaGetLastError());
   count_launches(ctx, 2);
   return PTG_OK;

@@ -51,6 +51,7 @@ struct T3Params {
   KrDevTc before, after;
   float *partial;  // [nsplit][Q][N]
   int *err;
+  const int *skip;  // nonzero: return at once (Contraction::skip)
 };
 
 // x rounded to the nearest TF32 value (ties away from zero): exact in TF32, and lo = x - hi is
@@ -84,6 +85,7 @@ __device__ __forceinline__ void fail_timeout(volatile int *abort_flag, int *err)
 
 __global__ void __launch_bounds__(T3_THREADS, 1)
 mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm) {
+  if (prm.skip && *prm.skip) return;   // before any barrier or TMEM allocation
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int N = prm.N;
@@ -382,7 +384,8 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
 }
 
 __global__ void tc32_reduce_kernel(const float *__restrict__ partial, int nsplit, int64_t Q, int N,
-                                   int64_t q_write, int R, float *__restrict__ out) {
+                                   int64_t q_write, int R, float *__restrict__ out, const int *skip) {
+  if (skip && *skip) return;
   const int64_t n = q_write * R;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
        idx += (int64_t)gridDim.x * blockDim.x) {
@@ -481,6 +484,7 @@ int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction
   PTG_TRY(ctx->scratch.ensure(part_bytes));
   prm.partial = reinterpret_cast<float *>(ctx->scratch.ptr);
   prm.err = ctx->dev_err;
+  prm.skip = c.skip;
   const size_t smem = tc32_smem_bytes(prm.N);
   if (smem > ctx->smem_optin) return set_error(PTG_ERR_UNSUPPORTED, "tensor-core FP32 MTTKRP: shared memory");
   PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -492,7 +496,7 @@ int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction
   const int64_t n = c.q_write * R;
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->sm_count * 8);
   tc32_reduce_kernel<<<std::max(blocks, 1), 256, 0, stream>>>(prm.partial, (int)nsplit, c.Q, prm.N, c.q_write,
-                                                              R, out);
+                                                              R, out, c.skip);
   PTG_CUDA(cudaGetLastError());
   count_launches(ctx, 2);
   return PTG_OK;
