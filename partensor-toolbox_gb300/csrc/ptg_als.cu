@@ -36,6 +36,8 @@ struct AlsBuffers {
                           // [4N], [4N + 1]: the line-search decision (accel_select_kernel)
   int *isc = nullptr;     // [N][2]: iterations, repaired; [2N]: the line search's stop gate
   double *W = nullptr;    // R x R FP64: Z^{-1} or (M^T M)^{-1/2} (other constraints)
+  double *cpart = nullptr;        // launch_cost_terms partials
+  unsigned *cticket = nullptr;    // and its ticket (zero between launches)
   void *base = nullptr;
 
   int alloc(const int64_t *dims, int order, int rank, int64_t rows_left = 0, int64_t rows_right = 0) {
@@ -70,6 +72,8 @@ struct AlsBuffers {
     const size_t o_d = take(sizeof(double) * (4 * N + 2));
     const size_t o_i = take(sizeof(int) * (2 * N + 2));
     const size_t o_W = take(sizeof(double) * R * R);
+    const size_t o_cp = take(sizeof(double) * kCostPartials);
+    const size_t o_ct = take(sizeof(unsigned));
     cudaError_t e = cudaMalloc(&base, off);
     if (e != cudaSuccess) {
       base = nullptr;
@@ -91,6 +95,10 @@ struct AlsBuffers {
     dsc = (double *)(b + o_d);
     isc = (int *)(b + o_i);
     W = (double *)(b + o_W);
+    cpart = (double *)(b + o_cp);
+    cticket = (unsigned *)(b + o_ct);
+    e = cudaMemset(cticket, 0, sizeof(unsigned));
+    if (e != cudaSuccess) return cuda_error(e, "cudaMemset(ALS ticket)", __FILE__, __LINE__);
     return PTG_OK;
   }
   ~AlsBuffers() {
@@ -243,7 +251,8 @@ struct Runner {
     Contraction c = mttkrp_contraction(X, factors, last);
     c.skip = skip;
     PTG_TRY(contraction_launch(ctx, X, c, b.R, b.M, S));
-    PTG_TRY(launch_cost_terms(b.M, factors[last], b.rows[last], grams, b.N, b.R, b.dsc + 2, S));
+    PTG_TRY(launch_cost_terms(b.M, factors[last], b.rows[last], grams, b.N, b.R, b.dsc + 2,
+                              CostScratch{b.cpart, b.cticket}, S));
     count_launches(ctx, 1);
     return PTG_OK;
   }
@@ -313,7 +322,8 @@ struct Runner {
     count_launches(ctx, 2);
     PTG_CUDA(cudaMemsetAsync(b.isc + 2 * n, 0, 2 * sizeof(int), S));
     if (n == N - 1) {
-      PTG_TRY(launch_cost_terms(b.M, b.fac[n], b.rows[n], b.gram, N, R, b.dsc + 4 * n, S));
+      PTG_TRY(launch_cost_terms(b.M, b.fac[n], b.rows[n], b.gram, N, R, b.dsc + 4 * n,
+                                CostScratch{b.cpart, b.cticket}, S));
       count_launches(ctx, 1);
     }
     return PTG_OK;

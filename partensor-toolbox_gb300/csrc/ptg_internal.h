@@ -252,8 +252,15 @@ int launch_accel_combine(const float *const *cur, const float *const *old, float
 int launch_update_unconstrained(ptg_ctx *ctx, const float *M, float *A, int I, int R, const NnlsParams *np,
                                 double *W, cudaStream_t s);
 int launch_update_orthogonal(ptg_ctx *ctx, const float *M, float *A, int I, int R, double *W, cudaStream_t s);
+// scratch of launch_cost_terms: 2 doubles per CTA and a ticket word that starts at zero (the
+// kernel leaves it at zero)
+struct CostScratch {
+  double *part;       // kCostPartials doubles
+  unsigned *ticket;
+};
+constexpr int kCostPartials = 64;
 int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const float *const *grams,
-                      int order, int R, double *out2, cudaStream_t stream);
+                      int order, int R, double *out2, CostScratch scratch, cudaStream_t stream);
 
 // Batched many-instance CPD (ptg_batched.cu, ptg_solve.cu).
 struct EigDesc {            // eigenbounds of one instance and mode

@@ -961,16 +961,39 @@ int launch_accel_combine(const float *const *cur, const float *const *old, float
 }
 
 // ---- FP64 cost terms for a given point: <M, A_last> and sum(Z .* G_last) ----
-__global__ void cost_terms_kernel(const float *__restrict__ M, const float *__restrict__ A, int64_t n,
-                                  GramPtrs gp, int order, int R, double *out2) {
-  __shared__ double red[32];
+// <M, A> over the last factor and sum(Z .* G) over the Grams in FP64 (the cost cancels
+// catastrophically).  kCostBlocks CTAs each sum a contiguous range of <M, A> (eight elements of
+// a thread in flight, added in order) and a strided share of sum(Z .* G); the CTA that finishes
+// last adds the partials in CTA order, so the result does not depend on timing.
+constexpr int kCostBlocks = 32, kCostThreads = 256;
+static_assert(2 * kCostBlocks <= kCostPartials, "cost-term partials");
+
+__global__ void __launch_bounds__(kCostThreads) cost_terms_kernel(const float *__restrict__ M,
+                                                                 const float *__restrict__ A, int64_t n,
+                                                                 GramPtrs gp, int order, int R, double *part,
+                                                                 unsigned *ticket, double *out2) {
+  __shared__ double red[2][kCostThreads / 32];
+  __shared__ bool is_last;
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t i0 = blockIdx.x * chunk, i1 = min(n, i0 + chunk);
   double s = 0.0;
-  for (int64_t idx = threadIdx.x; idx < n; idx += blockDim.x) s = fma((double)M[idx], (double)A[idx], s);
+  int64_t idx = i0 + threadIdx.x;
+  for (; idx + 7 * kCostThreads < i1; idx += 8 * kCostThreads) {
+    float m[8], a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      m[u] = __ldg(M + idx + u * kCostThreads);
+      a[u] = __ldg(A + idx + u * kCostThreads);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s = fma((double)m[u], (double)a[u], s);
+  }
+  for (; idx < i1; idx += kCostThreads) s = fma((double)M[idx], (double)A[idx], s);
   double h = 0.0;
-  for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
+  for (int k = blockIdx.x * kCostThreads + threadIdx.x; k < R * R; k += gridDim.x * kCostThreads) {
     double z = 1.0;
-    for (int k = order - 2; k >= 0; --k) z *= (double)gp.g[k][idx];
-    h = fma(z, (double)gp.g[order - 1][idx], h);
+    for (int j = order - 2; j >= 0; --j) z *= (double)gp.g[j][k];
+    h = fma(z, (double)gp.g[order - 1][k], h);
   }
   for (int o = 16; o > 0; o >>= 1) {
     s += __shfl_down_sync(0xffffffffu, s, o);
@@ -978,26 +1001,41 @@ __global__ void cost_terms_kernel(const float *__restrict__ M, const float *__re
   }
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    red[w] = s;
-    red[16 + w] = h;
+    red[0][w] = s;
+    red[1][w] = h;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     double a = 0.0, b = 0.0;
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-      a += red[i];
-      b += red[16 + i];
+    for (int i = 0; i < kCostThreads / 32; ++i) {
+      a += red[0][i];
+      b += red[1][i];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+    __threadfence();
+    is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (is_last && threadIdx.x == 0) {
+    __threadfence();
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < (int)gridDim.x; ++i) {
+      a += __ldcg(part + 2 * i);
+      b += __ldcg(part + 2 * i + 1);
     }
     out2[0] = a;
     out2[1] = b;
+    *ticket = 0u;   // ready for the next launch on the stream
   }
 }
 
 int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const float *const *grams,
-                      int order, int R, double *out2, cudaStream_t stream) {
+                      int order, int R, double *out2, CostScratch scratch, cudaStream_t stream) {
   GramPtrs gp{};
   for (int k = 0; k < order; ++k) gp.g[k] = grams[k];
-  cost_terms_kernel<<<1, 512, 0, stream>>>(M, A_last, I_last * R, gp, order, R, out2);
+  cost_terms_kernel<<<kCostBlocks, kCostThreads, 0, stream>>>(M, A_last, I_last * R, gp, order, R, scratch.part,
+                                                             scratch.ticket, out2);
   PTG_CUDA(cudaGetLastError());
   return PTG_OK;
 }
