@@ -245,12 +245,13 @@ struct Runner {
   // the line-search point's cost terms (one last-mode MTTKRP in the Gram form) into
   // b.dsc[2..3], queued
   int point_cost_enqueue(const ptg_tensor *X, float *const *factors, float *const *grams,
-                         const int *skip = nullptr) {
+                         const int *skip = nullptr, cudaEvent_t grams_ready = nullptr) {
     cudaStream_t S = ctx->stream;
     const int last = b.N - 1;
     Contraction c = mttkrp_contraction(X, factors, last);
     c.skip = skip;
     PTG_TRY(contraction_launch(ctx, X, c, b.R, b.M, S));
+    if (grams_ready) PTG_CUDA(cudaStreamWaitEvent(S, grams_ready, 0));
     PTG_TRY(launch_cost_terms(b.M, factors[last], b.rows[last], grams, b.N, b.R, b.dsc + 2,
                               CostScratch{b.cpart, b.cticket}, S));
     count_launches(ctx, 1);
@@ -515,7 +516,15 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
       if (ao_iter > 1) {
         const double step = std::pow((double)(ao_iter + 1), 1.0 / (double)opt.accel_coeff);
         PTG_TRY(launch_accel_combine(b.fac, b.old, b.acc, b.rows, N, rank, step, S));
-        for (int k = 0; k < N; ++k) PTG_TRY(launch_gram(b.acc[k], b.rows[k], rank, b.gacc[k], b.gpart, S));
+        // the accelerated factors' Grams on the side stream, beside the point's MTTKRP: only the
+        // point's cost terms need them
+        cudaStream_t T = ctx->side;
+        PTG_CUDA(cudaEventRecord(ctx->ev_fork, S));
+        PTG_CUDA(cudaStreamWaitEvent(T, ctx->ev_fork, 0));
+        const bool beside_tc = contraction_uses_tc(ctx, Xa, rank);
+        for (int k = 0; k < N; ++k)
+          PTG_TRY(launch_gram(b.acc[k], b.rows[k], rank, b.gacc[k], b.gpart, T, beside_tc));
+        PTG_CUDA(cudaEventRecord(ctx->ev_join, T));
         count_launches(ctx, 1 + 2 * N);
         for (int k = 0; k < N; ++k)
           PTG_CUDA(cudaMemcpyAsync(b.old[k], b.fac[k], sizeof(float) * b.rows[k] * rank,
@@ -524,7 +533,7 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
         stop_gate_kernel<<<1, 1, 0, S>>>(b.dsc, N - 1, frob, opt.threshold_error, ao_iter, opt.max_iter, gate);
         PTG_CUDA(cudaGetLastError());
         count_launches(ctx, 1);
-        PTG_TRY(run.point_cost_enqueue(Xa, b.acc, b.gacc, gate));
+        PTG_TRY(run.point_cost_enqueue(Xa, b.acc, b.gacc, gate, ctx->ev_join));
         PTG_TRY(run.select_enqueue(frob, opt.threshold_error, ao_iter, opt.max_iter));
         sel_pending = true;
         sel_sweep = ntrace;

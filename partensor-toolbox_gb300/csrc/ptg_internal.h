@@ -240,7 +240,8 @@ int launch_nnls_full(ptg_ctx *ctx, const float *M, float *A, int I, int R, const
                      int *iters_out, int *repaired_out, cudaStream_t stream,
                      const WarmArgs &warm = WarmArgs());
 size_t gram_scratch_floats(int I, int R);
-int launch_gram(const float *A, int I, int R, float *G, float *part, cudaStream_t stream);
+// beside_tc: the launch runs beside a tensor-core MTTKRP and takes its shared-memory carveout
+int launch_gram(const float *A, int I, int R, float *G, float *part, cudaStream_t stream, bool beside_tc = false);
 int launch_normalize(float *const *fac, float *const *gram, const int *rows, int order, int weight,
                      int R, cudaStream_t stream);
 int launch_accel_combine(const float *const *cur, const float *const *old, float *const *acc,

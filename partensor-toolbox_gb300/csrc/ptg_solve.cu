@@ -809,10 +809,14 @@ int launch_nnls_full(ptg_ctx *ctx, const float *M, float *A, int I, int R, const
   return set_error(PTG_ERR_UNSUPPORTED, "factor has too many rows for the NNLS kernel");
 }
 
-int launch_gram(const float *A, int I, int R, float *G, float *part, cudaStream_t stream) {
+int launch_gram(const float *A, int I, int R, float *G, float *part, cudaStream_t stream, bool beside_tc) {
   const int nb = (I + kGramRowsPerBlock - 1) / kGramRowsPerBlock;
   const size_t smem = sizeof(float) * kGramRowsPerBlock * R;
   PTG_CUDA(cudaFuncSetAttribute(gram_partial_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // beside the tensor-core MTTKRP the same carveout, so that the CTAs share SMs with it
+  const int carve = beside_tc ? (int)cudaSharedmemCarveoutMaxShared : (int)cudaSharedmemCarveoutDefault;
+  PTG_CUDA(cudaFuncSetAttribute(gram_partial_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
+  PTG_CUDA(cudaFuncSetAttribute(sum_rr_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, carve));
   gram_partial_kernel<<<nb, 256, smem, stream>>>(A, I, R, part);
   sum_rr_kernel<<<(R * R + 255) / 256, 256, 0, stream>>>(part, nb, R * R, G);
   PTG_CUDA(cudaGetLastError());
