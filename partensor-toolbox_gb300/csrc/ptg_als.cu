@@ -524,11 +524,13 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
         const bool beside_tc = contraction_uses_tc(ctx, Xa, rank);
         for (int k = 0; k < N; ++k)
           PTG_TRY(launch_gram(b.acc[k], b.rows[k], rank, b.gacc[k], b.gpart, T, beside_tc));
-        PTG_CUDA(cudaEventRecord(ctx->ev_join, T));
-        count_launches(ctx, 1 + 2 * N);
+        // old <- fac there too: nothing writes the factors before accel_select_kernel, which
+        // runs after the join
         for (int k = 0; k < N; ++k)
           PTG_CUDA(cudaMemcpyAsync(b.old[k], b.fac[k], sizeof(float) * b.rows[k] * rank,
-                                   cudaMemcpyDeviceToDevice, S));
+                                   cudaMemcpyDeviceToDevice, T));
+        PTG_CUDA(cudaEventRecord(ctx->ev_join, T));
+        count_launches(ctx, 1 + 2 * N);
         int *gate = b.isc + 2 * N;
         stop_gate_kernel<<<1, 1, 0, S>>>(b.dsc, N - 1, frob, opt.threshold_error, ao_iter, opt.max_iter, gate);
         PTG_CUDA(cudaGetLastError());

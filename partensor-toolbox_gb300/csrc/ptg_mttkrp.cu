@@ -746,8 +746,11 @@ int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, 
     return set_error(PTG_ERR_UNSUPPORTED, "contraction extent exceeds 2^32");
   if (c.P > 1 && (c.P % 8) != 0)
     return set_error(PTG_ERR_INVALID, "internal: P must be a multiple of 8");
+  // A launch that a device word may cancel (Contraction::skip) stays out of the MTTKRP
+  // statistics: the host cannot tell whether it did the work its bytes stand for.
+  const bool timed = c.skip == nullptr;
   cudaEvent_t ev = nullptr;
-  PTG_TRY(stats_begin(ctx, stream, &ev));
+  if (timed) PTG_TRY(stats_begin(ctx, stream, &ev));
   int rc;
   const bool tc = contraction_uses_tc(ctx, t, R);
   if (t->dtype == PTG_F32 && tc)
@@ -761,6 +764,7 @@ int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, 
   else
     return set_error(PTG_ERR_UNSUPPORTED, "tensor dtype");
   if (rc != PTG_OK) return rc;
+  if (!timed) return PTG_OK;
   double numel = 1.0;
   for (int k = 0; k < t->order; ++k) numel *= (double)t->dims[k];
   return stats_end(ctx, stream, ev, contraction_bytes(t, c, R), 2.0 * numel * R, tc);
