@@ -76,8 +76,9 @@ typedef enum {
                              with the contraction length) */,
   PTG_OPT_NNLS_CLUSTER = 2 /* CTAs of the NNLS thread-block cluster: 0 auto (16 where the device
                              schedules it, else 8), or 2, 4, 8, 16 */,
-  PTG_OPT_GTC_ROWS = 3 /* sparse row solver of the stochastic form: 0 auto (one warp per row
-                          for rank <= 32, else one CTA per row), 1 one CTA per row */
+  PTG_OPT_GTC_ROWS = 3 /* sparse row solver of the nonnegative GTC modes: 0 auto (one warp per
+                          row for rank <= 32, else one CTA per row), 1 one CTA per row; both
+                          give the same bits */
 } ptg_option;
 int ptg_ctx_set_option(ptg_ctx *ctx, int option, long long value);
 

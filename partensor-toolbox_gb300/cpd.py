@@ -110,8 +110,8 @@ class Context:
         check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_NNLS_CLUSTER, int(size)))
 
     def set_gtc_rows(self, solver: str):
-        """Row solver of the stochastic sparse completion: "auto" (one warp per row for
-        rank <= 32) or "cta" (one CTA per row)."""
+        """Row solver of the sparse completion's nonnegative modes: "auto" (one warp per row
+        for rank <= 32) or "cta" (one CTA per row); both give the same bits."""
         check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_GTC_ROWS, {"auto": 0, "cta": 1}[solver]))
 
     def enable_stats(self, on: bool = True):

@@ -11,8 +11,9 @@
 //   entries once, accumulates m_i = sum x kr and H_i = sum kr kr^T, runs PowerMethod on H_i
 //   and the max_nesterov_iter projected Nesterov steps with grad = H_i y - m_i + lambda y;
 //   dynamic_blocksize::StochasticNesterovMNLS (include/NesterovMNLS.hpp:431-547): the same per
-//   row on a contiguous block of floor(c * nnz_i) entries at a counter-hashed pivot, one warp
-//   per row at rank <= 32 (H_i in registers, no CTA barrier), else one CTA per row;
+//   row on a contiguous block of floor(c * nnz_i) entries at a counter-hashed pivot; both
+//   forms run one warp per row at rank <= 32 (H_i in registers, no CTA barrier), else (and for
+//   the ridge solve) one CTA per row;
 //   the GTC cost (include/Gtc.hpp:184-214) as per-row FP64 partial sums added in row order.
 // No global atomics on the data path; every reduction is in a fixed order.
 #include <algorithm>
@@ -636,9 +637,9 @@ __global__ void __launch_bounds__(GT_THREADS) gtc_row_kernel(const RowArgs a) {
   }
 }
 
-// ---- one warp per row (rank <= 32): dynamic_blocksize::StochasticNesterovMNLS ----
+// ---- one warp per row (rank <= 32): both Nesterov forms of the nonnegative modes ----
 // The one-CTA kernel keeps three of its four warps waiting at barriers while warp 0 runs the
-// power method and the step.  Here each warp owns a row: lane r holds row r of the sampled H_i
+// power method and the steps.  Here each warp owns a row: lane r holds row r of the sampled H_i
 // in registers (H is symmetric, so it is also column r), m_i[r], a_i[r] and the extrapolated
 // y[r]; a vector every lane needs (a Khatri-Rao row, the power iterate, y) passes through the
 // warp's own shared-memory slots, and only __syncwarp orders them.  The arithmetic and its
@@ -704,8 +705,124 @@ __device__ __forceinline__ float power_method_lane(const float (&H)[32], float *
 // NJ = order - 1 other modes; VEC: R is a multiple of 4, so every factor row starts on a
 // 16-byte boundary and 8 lanes gather one entry's Khatri-Rao row as float4s (4 entries per
 // warp instruction); otherwise lane r gathers rank r of one entry at a time.
+// H_i = sum kr kr^T and m_i = sum x kr over the entries [s1, s1 + nb) of a row, by one warp.
+// Lane (rg, cg) = (lane / 4, lane % 4) accumulates the 4 x 8 block of H_i at rows 4 rg..,
+// columns 8 cg..: 3 float4 reads per entry for 32 FMAs, where a whole row per lane needs 8
+// broadcast reads and shared memory, not the FMA pipe, sets the pace.  On return lane r holds
+// row r of H_i in H (through the staging buffer) and m_i[r] in m.
 template <int NJ, bool VEC>
-__global__ void __launch_bounds__(GW_WARPS * 32, 7) gtc_stoch_warp_kernel(const RowArgs a, int64_t rows) {
+__device__ __forceinline__ void warp_row_hessian(const RowArgs &a, WarpRowShared &sh, int64_t s1, int64_t nb,
+                                                 float (&H)[32], float &m) {
+  const int lane = threadIdx.x & 31, R = a.R;
+  const bool own = lane < R;
+  const int rg = lane >> 2, cg = lane & 3;
+  float Hb[4][8];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) Hb[k][j] = 0.0f;
+  float m4[4] = {0.0f, 0.0f, 0.0f, 0.0f};   // m_i at rows 4 rg.. (the 4 lanes of a row group alike)
+  for (int64_t s0 = s1; s0 < s1 + nb; s0 += GW_CHUNK) {
+    const int cnt = (int)(s1 + nb - s0 < GW_CHUNK ? s1 + nb - s0 : GW_CHUNK);
+    // lane e reads entry e's rows in the other modes and its value
+    if (lane < cnt) {
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) sh.rows[j][lane] = a.oidx[(int64_t)j * a.nnz + s0 + lane];
+      sh.xv[lane] = a.vals[s0 + lane];
+    }
+    __syncwarp();
+    // each entry's Khatri-Rao row, the product taken from the last mode down (kr_value);
+    // ranks >= R are zero
+    if (VEC) {
+      const int sub = lane >> 3, r4 = (lane & 7) * 4;
+#pragma unroll 2
+      for (int e = sub; e < cnt; e += 4) {
+        float4 kv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (r4 < R) {
+          kv = __ldg(reinterpret_cast<const float4 *>(a.fac[NJ - 1] + (size_t)sh.rows[NJ - 1][e] * R + r4));
+#pragma unroll
+          for (int j = NJ - 2; j >= 0; --j) {
+            const float4 f = __ldg(reinterpret_cast<const float4 *>(a.fac[j] + (size_t)sh.rows[j][e] * R + r4));
+            kv.x *= f.x;
+            kv.y *= f.y;
+            kv.z *= f.z;
+            kv.w *= f.w;
+          }
+        }
+        *reinterpret_cast<float4 *>(&sh.kr[e][r4]) = kv;
+      }
+    } else {
+#pragma unroll 4
+      for (int e = 0; e < cnt; ++e) {
+        float kv = 0.0f;
+        if (own) {
+          kv = __ldg(a.fac[NJ - 1] + (size_t)sh.rows[NJ - 1][e] * R + lane);
+#pragma unroll
+          for (int j = NJ - 2; j >= 0; --j) kv *= __ldg(a.fac[j] + (size_t)sh.rows[j][e] * R + lane);
+        }
+        sh.kr[e][lane] = kv;
+      }
+    }
+    __syncwarp();
+#pragma unroll 2
+    for (int e = 0; e < cnt; ++e) {
+      const float4 ra = *reinterpret_cast<const float4 *>(&sh.kr[e][4 * rg]);
+      const float rk[4] = {ra.x, ra.y, ra.z, ra.w};
+      const float xe = sh.xv[e];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) m4[k] = fmaf(xe, rk[k], m4[k]);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const float4 cb = *reinterpret_cast<const float4 *>(&sh.kr[e][8 * cg + 4 * h]);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          Hb[k][4 * h] = fmaf(rk[k], cb.x, Hb[k][4 * h]);
+          Hb[k][4 * h + 1] = fmaf(rk[k], cb.y, Hb[k][4 * h + 1]);
+          Hb[k][4 * h + 2] = fmaf(rk[k], cb.z, Hb[k][4 * h + 2]);
+          Hb[k][4 * h + 3] = fmaf(rk[k], cb.w, Hb[k][4 * h + 3]);
+        }
+      }
+    }
+    __syncwarp();
+  }
+  // H_i to one row per lane (row r in lane r) through the staging buffer
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      *reinterpret_cast<float4 *>(&sh.kr[4 * rg + k][8 * cg + 4 * h]) =
+          make_float4(Hb[k][4 * h], Hb[k][4 * h + 1], Hb[k][4 * h + 2], Hb[k][4 * h + 3]);
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const float4 t = *reinterpret_cast<const float4 *>(&sh.kr[lane][4 * q]);
+    H[4 * q] = t.x;
+    H[4 * q + 1] = t.y;
+    H[4 * q + 2] = t.z;
+    H[4 * q + 3] = t.w;
+  }
+  __syncwarp();   // the staging buffer is gathered into again by the next block
+  m = cg == 0 ? m4[0] : cg == 1 ? m4[1] : cg == 2 ? m4[2] : m4[3];   // m_i[lane]
+}
+
+// one projected Nesterov step of this lane's column: grad = H y - m + lambda (y + prox a)
+__device__ __forceinline__ void warp_row_step(const float (&H)[32], float *v, float m, bool own, float lam,
+                                              float invL, float beta, float prox, float &av, float &yv) {
+  const int lane = threadIdx.x & 31;
+  v[lane] = yv;
+  __syncwarp();
+  const float g = row_dot(H, v, step_grad0(m, lam, yv, prox, av));
+  const float na = own ? step_project(yv, invL, g) : 0.0f;
+  __syncwarp();
+  yv = step_extrapolate(beta, na, av);
+  av = na;
+}
+
+// STOCH: dynamic_blocksize::StochasticNesterovMNLS, a fresh sampled block per inner step;
+// else local_L::NesterovMNLS, H_i over all the row's entries, then max_iter steps
+// (nonnegative modes; the ridge solve of unconstrained modes stays on the one-CTA kernel).
+template <int NJ, bool VEC, bool STOCH>
+__global__ void __launch_bounds__(GW_WARPS * 32, 7) gtc_warp_kernel(const RowArgs a, int64_t rows) {
   __shared__ __align__(16) WarpRowShared shw[GW_WARPS];
   const int lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * GW_WARPS + (threadIdx.x >> 5);
@@ -716,138 +833,54 @@ __global__ void __launch_bounds__(GW_WARPS * 32, 7) gtc_stoch_warp_kernel(const 
   const int64_t p0 = a.ptr[i], cnt_row = a.ptr[i + 1] - p0;
   float av = own ? a.A[i * R + lane] : 0.0f;
   float yv = av;
-  const int64_t b = (int64_t)(a.c * (float)cnt_row);   // floor(c * nnz_i)
-  if (b > 0) {
-    for (int it = 0; it < a.max_iter; ++it) {
-      const unsigned long long draw = splitmix_draw(a.seed, (unsigned long long)a.outer,
-                                                    (unsigned long long)a.mode, (unsigned long long)it,
-                                                    (unsigned long long)i);
-      const int64_t s1 = p0 + (int64_t)(draw % (unsigned long long)(cnt_row - b + 1));
-      // lane (rg, cg) = (lane / 4, lane % 4) accumulates the 4 x 8 block of H_i at rows 4 rg..,
-      // columns 8 cg..: 3 float4 reads per entry for 32 FMAs, where a whole row per lane needs 8
-      // broadcast reads and shared memory, not the FMA pipe, sets the pace
-      const int rg = lane >> 2, cg = lane & 3;
-      float Hb[4][8];
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-#pragma unroll
-        for (int j = 0; j < 8; ++j) Hb[k][j] = 0.0f;
-      float m4[4] = {0.0f, 0.0f, 0.0f, 0.0f};   // m_i at rows 4 rg.. (the 4 lanes of a row group alike)
-      for (int64_t s0 = s1; s0 < s1 + b; s0 += GW_CHUNK) {
-        const int cnt = (int)(s1 + b - s0 < GW_CHUNK ? s1 + b - s0 : GW_CHUNK);
-        // lane e reads entry e's rows in the other modes and its value
-        if (lane < cnt) {
-#pragma unroll
-          for (int j = 0; j < NJ; ++j) sh.rows[j][lane] = a.oidx[(int64_t)j * a.nnz + s0 + lane];
-          sh.xv[lane] = a.vals[s0 + lane];
-        }
-        __syncwarp();
-        // each entry's Khatri-Rao row, the product taken from the last mode down (kr_value);
-        // ranks >= R are zero
-        if (VEC) {
-          const int sub = lane >> 3, r4 = (lane & 7) * 4;
-#pragma unroll 2
-          for (int e = sub; e < cnt; e += 4) {
-            float4 kv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (r4 < R) {
-              kv = __ldg(reinterpret_cast<const float4 *>(a.fac[NJ - 1] + (size_t)sh.rows[NJ - 1][e] * R + r4));
-#pragma unroll
-              for (int j = NJ - 2; j >= 0; --j) {
-                const float4 f = __ldg(reinterpret_cast<const float4 *>(a.fac[j] + (size_t)sh.rows[j][e] * R + r4));
-                kv.x *= f.x;
-                kv.y *= f.y;
-                kv.z *= f.z;
-                kv.w *= f.w;
-              }
-            }
-            *reinterpret_cast<float4 *>(&sh.kr[e][r4]) = kv;
-          }
-        } else {
-#pragma unroll 4
-          for (int e = 0; e < cnt; ++e) {
-            float kv = 0.0f;
-            if (own) {
-              kv = __ldg(a.fac[NJ - 1] + (size_t)sh.rows[NJ - 1][e] * R + lane);
-#pragma unroll
-              for (int j = NJ - 2; j >= 0; --j) kv *= __ldg(a.fac[j] + (size_t)sh.rows[j][e] * R + lane);
-            }
-            sh.kr[e][lane] = kv;
-          }
-        }
-        __syncwarp();
-#pragma unroll 2
-        for (int e = 0; e < cnt; ++e) {
-          const float4 ra = *reinterpret_cast<const float4 *>(&sh.kr[e][4 * rg]);
-          const float rk[4] = {ra.x, ra.y, ra.z, ra.w};
-          const float xe = sh.xv[e];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) m4[k] = fmaf(xe, rk[k], m4[k]);
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const float4 cb = *reinterpret_cast<const float4 *>(&sh.kr[e][8 * cg + 4 * h]);
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              Hb[k][4 * h] = fmaf(rk[k], cb.x, Hb[k][4 * h]);
-              Hb[k][4 * h + 1] = fmaf(rk[k], cb.y, Hb[k][4 * h + 1]);
-              Hb[k][4 * h + 2] = fmaf(rk[k], cb.z, Hb[k][4 * h + 2]);
-              Hb[k][4 * h + 3] = fmaf(rk[k], cb.w, Hb[k][4 * h + 3]);
-            }
-          }
-        }
-        __syncwarp();
+  float H[32], m;
+  if (STOCH) {
+    const int64_t b = (int64_t)(a.c * (float)cnt_row);   // floor(c * nnz_i)
+    if (b > 0) {
+      for (int it = 0; it < a.max_iter; ++it) {
+        const unsigned long long draw = splitmix_draw(a.seed, (unsigned long long)a.outer,
+                                                      (unsigned long long)a.mode, (unsigned long long)it,
+                                                      (unsigned long long)i);
+        const int64_t s1 = p0 + (int64_t)(draw % (unsigned long long)(cnt_row - b + 1));
+        warp_row_hessian<NJ, VEC>(a, sh, s1, b, H, m);
+        float invL, beta;
+        step_constants(power_method_lane(H, sh.v, own, 1e-3f), a.lambda, invL, beta);
+        // grad = sum (kr.y - x) kr + lambda (y + a) = H y - m + lambda (y + a)
+        // (include/NesterovMNLS.hpp:516, :525)
+        warp_row_step(H, sh.v, m, own, a.lambda, invL, beta, 1.0f, av, yv);
       }
-      // H_i to one row per lane (row r in lane r) through the staging buffer
-#pragma unroll
-      for (int k = 0; k < 4; ++k)
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-          *reinterpret_cast<float4 *>(&sh.kr[4 * rg + k][8 * cg + 4 * h]) =
-              make_float4(Hb[k][4 * h], Hb[k][4 * h + 1], Hb[k][4 * h + 2], Hb[k][4 * h + 3]);
-      __syncwarp();
-      float H[32];
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const float4 t = *reinterpret_cast<const float4 *>(&sh.kr[lane][4 * q]);
-        H[4 * q] = t.x;
-        H[4 * q + 1] = t.y;
-        H[4 * q + 2] = t.z;
-        H[4 * q + 3] = t.w;
-      }
-      __syncwarp();   // the staging buffer is gathered into again by the next block
-      const float m = cg == 0 ? m4[0] : cg == 1 ? m4[1] : cg == 2 ? m4[2] : m4[3];   // m_i[lane]
-      float invL, beta;
-      step_constants(power_method_lane(H, sh.v, own, 1e-3f), a.lambda, invL, beta);
-      // grad = H y - m + lambda (y + a) (include/NesterovMNLS.hpp:516, :525)
-      sh.v[lane] = yv;
-      __syncwarp();
-      const float g = row_dot(H, sh.v, step_grad0(m, a.lambda, yv, 1.0f, av));
-      const float na = own ? step_project(yv, invL, g) : 0.0f;
-      __syncwarp();
-      yv = step_extrapolate(beta, na, av);
-      av = na;
     }
+  } else {
+    warp_row_hessian<NJ, VEC>(a, sh, p0, cnt_row, H, m);   // an empty row: H = 0, m = 0
+    float invL, beta;
+    step_constants(cnt_row > 0 ? power_method_lane(H, sh.v, own, 1e-3f) : 0.0f, a.lambda, invL, beta);
+    for (int it = 0; it < a.max_iter; ++it) warp_row_step(H, sh.v, m, own, a.lambda, invL, beta, 0.0f, av, yv);
   }
   if (own) a.A[i * R + lane] = av;
 }
 
 template <int NJ>
-void launch_stoch_warp_nj(const RowArgs &a, int64_t rows, cudaStream_t S) {
+void launch_warp_rows_nj(const RowArgs &a, int64_t rows, cudaStream_t S) {
   const unsigned grid = (unsigned)((rows + GW_WARPS - 1) / GW_WARPS);
-  if (a.R % 4 == 0)
-    gtc_stoch_warp_kernel<NJ, true><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
-  else
-    gtc_stoch_warp_kernel<NJ, false><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+  const bool vec = a.R % 4 == 0;
+  if (a.stochastic) {
+    if (vec) gtc_warp_kernel<NJ, true, true><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+    else gtc_warp_kernel<NJ, false, true><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+  } else {
+    if (vec) gtc_warp_kernel<NJ, true, false><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+    else gtc_warp_kernel<NJ, false, false><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+  }
 }
 
-void launch_stoch_warp(const RowArgs &a, int64_t rows, cudaStream_t S) {
+void launch_warp_rows(const RowArgs &a, int64_t rows, cudaStream_t S) {
   switch (a.N - 1) {
-    case 1: launch_stoch_warp_nj<1>(a, rows, S); break;
-    case 2: launch_stoch_warp_nj<2>(a, rows, S); break;
-    case 3: launch_stoch_warp_nj<3>(a, rows, S); break;
-    case 4: launch_stoch_warp_nj<4>(a, rows, S); break;
-    case 5: launch_stoch_warp_nj<5>(a, rows, S); break;
-    case 6: launch_stoch_warp_nj<6>(a, rows, S); break;
-    default: launch_stoch_warp_nj<7>(a, rows, S); break;
+    case 1: launch_warp_rows_nj<1>(a, rows, S); break;
+    case 2: launch_warp_rows_nj<2>(a, rows, S); break;
+    case 3: launch_warp_rows_nj<3>(a, rows, S); break;
+    case 4: launch_warp_rows_nj<4>(a, rows, S); break;
+    case 5: launch_warp_rows_nj<5>(a, rows, S); break;
+    case 6: launch_warp_rows_nj<6>(a, rows, S); break;
+    default: launch_warp_rows_nj<7>(a, rows, S); break;
   }
 }
 
@@ -1182,8 +1215,8 @@ int ptg_gtc(ptg_ctx *ctx, int order, const int64_t *dims, int64_t nnz, const int
       RowArgs a = make_args(n);
       a.outer = ao_iter;
       a.ridge = ridge ? 1 : 0;
-      if (opt->stochastic && R <= 32 && ctx->gtc_rows == 0)
-        launch_stoch_warp(a, dims[n], S);
+      if (R <= 32 && !a.ridge && ctx->gtc_rows == 0)
+        launch_warp_rows(a, dims[n], S);
       else
         gtc_row_kernel<<<(unsigned)dims[n], GT_THREADS, smem, S>>>(a);
       count_launches(ctx, 1);

@@ -140,6 +140,27 @@ def test_gtc_stochastic_row_solvers_agree(pkg, ctx, R):
     assert out["auto"].rel_costFunction == out["cta"].rel_costFunction
 
 
+@pytest.mark.parametrize("R", [3, 17, 32])
+def test_gtc_full_row_solvers_agree(pkg, ctx, R):
+    """local_L Nesterov with one warp per row (rank <= 32) and with one CTA per row: the same
+    FMAs in the same order, the same bits (rows with no entries included)."""
+    dims = (70, 60, 50)
+    idx, vals, init = _problem(dims, 9000, R, 25)
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=3, lambdas=[1e-3] * 3,
+                          factorsInit=init)
+    out = {}
+    for solver in ("auto", "cta"):
+        c = pkg.Context(0)
+        try:
+            c.set_gtc_rows(solver)
+            out[solver] = pkg.gtc_coo(idx, vals, o, ctx=c)
+        finally:
+            c.close()
+    for k in range(3):
+        assert np.array_equal(out["auto"].factors[k], out["cta"].factors[k]), k
+    assert out["auto"].rel_costFunction == out["cta"].rel_costFunction
+
+
 @pytest.mark.parametrize("R", [32, 40])
 def test_gtc_stochastic_matches_oracle_rank(pkg, ctx, R):
     """Stochastic form at rank 32 (one warp per row) and 40 (one CTA per row) against the oracle.
