@@ -181,3 +181,30 @@ def test_gtc_stochastic_matches_oracle_rank(pkg, ctx, R):
     rel_ref = np.array([t["rel"] for t in ref.trace])
     assert np.max(np.abs(rel_gpu - rel_ref)) < 2e-4, (rel_gpu, rel_ref)
     assert oc.congruence(st.factors, ref.factors) >= 0.99
+
+
+@pytest.mark.parametrize("R", [6, 8])
+def test_gtc_4way_row_solvers(pkg, ctx, R):
+    """Order 4 (three other modes per entry; R = 8 gathers float4 rows, R = 6 scalars): the
+    warp-per-row and one-CTA solvers give the same bits in both forms, and the full form
+    follows the oracle within 2e-4 per iteration."""
+    dims = (16, 14, 12, 10)
+    idx, vals, init = _problem(dims, 6000, R, 31)
+    for stochastic in (False, True):
+        o = pkg.SparseOptions(order=4, rank=R, tnsDims=list(dims), max_iter=3, lambdas=[1e-3] * 4,
+                              c_stochastic_perc=0.2, seed=7, factorsInit=init)
+        out = {}
+        for solver in ("auto", "cta"):
+            c = pkg.Context(0)
+            try:
+                c.set_gtc_rows(solver)
+                out[solver] = pkg.gtc_coo(idx, vals, o, stochastic=stochastic, ctx=c)
+            finally:
+                c.close()
+        for k in range(4):
+            assert np.array_equal(out["auto"].factors[k], out["cta"].factors[k]), (stochastic, k)
+        if not stochastic:
+            ref = og.gtc(idx, vals, dims, R, og.SparseOptions(order=4, max_iter=3, lambdas=[1e-3] * 4), init)
+            rel_gpu = np.array([t["rel"] for t in out["auto"].trace])
+            rel_ref = np.array([t["rel"] for t in ref.trace])
+            assert np.max(np.abs(rel_gpu - rel_ref)) < 2e-4, (rel_gpu, rel_ref)
