@@ -98,3 +98,46 @@ def test_mlp_gradient_finite_differences():
         e[i] = 1e-6
         fd = (om.loss_and_grad(theta + e, X, T, din, h, dout)[0] - om.loss_and_grad(theta - e, X, T, din, h, dout)[0]) / 2e-6
         assert fd == pytest.approx(g[i], rel=1e-4, abs=1e-9)
+
+
+def test_ridge_update_minimises_the_row_objective():
+    """unconstraint_update (include/Gtc.hpp:275-315): each row minimises
+    sum over its entries (x - kr.a)^2 + lambda ||a||^2, so H a - m + lambda a = 0 and a equals
+    the least-squares solution of the stacked system [K; sqrt(lambda) I] a = [x; 0]."""
+    dims, R, lam = (12, 10, 9), 4, 1e-2
+    idx, vals, _ = og.make_gtc_problem(dims, 600, R, seed=41)
+    rng = np.random.default_rng(42)
+    factors = [rng.random((I, R)) for I in dims]
+    for mode in range(3):
+        mm = og.matricize(idx, vals, dims, mode)
+        M = og.sparse_mttkrp(factors, mm)
+        A = og.ridge_update(factors, mm, M, lam)
+        H = og.row_hessians(factors, mm)
+        kr = og.kr_rows(factors, mm)
+        for i in range(dims[mode]):
+            grad = H[i] @ A[i] - M[i] + lam * A[i]
+            assert np.abs(grad).max() < 1e-10 * max(1.0, np.abs(M[i]).max())
+            K = kr[mm.ptr[i]:mm.ptr[i + 1]]
+            x = mm.vals[mm.ptr[i]:mm.ptr[i + 1]]
+            stacked = np.vstack([K, np.sqrt(lam) * np.eye(R)])
+            ls = np.linalg.lstsq(stacked, np.concatenate([x, np.zeros(R)]), rcond=None)[0]
+            assert np.allclose(A[i], ls, rtol=1e-9, atol=1e-12)
+
+
+def test_local_l_nesterov_reaches_row_kkt():
+    """local_L::NesterovMNLS (include/NesterovMNLS.hpp:777-873) run long: every row meets the
+    KKT conditions of min (1/2) a^T (H + lambda I) a - m^T a over a >= 0."""
+    dims, R, lam = (10, 9, 8), 3, 1e-3
+    idx, vals, _ = og.make_gtc_problem(dims, 500, R, seed=43)
+    rng = np.random.default_rng(44)
+    factors = [rng.random((I, R)) for I in dims]
+    mm = og.matricize(idx, vals, dims, 0)
+    M = og.sparse_mttkrp(factors, mm)
+    A = og.local_L_nesterov(factors, mm, M, 3000, lam)
+    H = og.row_hessians(factors, mm)
+    assert (A >= 0).all()
+    for i in range(dims[0]):
+        grad = H[i] @ A[i] - M[i] + lam * A[i]
+        scale = max(1.0, np.abs(M[i]).max())
+        assert grad.min() > -1e-6 * scale                       # dual feasibility
+        assert np.abs(grad * A[i]).max() < 1e-6 * scale ** 2    # complementarity
