@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import dataclasses
 import math
+import os
 from typing import List, Sequence
 
 import torch
@@ -86,6 +87,82 @@ def make_cpd_problem(dims: Sequence[int], rank: int, seed: int, snr_db: float,
     gi = torch.Generator(device=device).manual_seed(int(seed + 1 if init_seed is None else init_seed))
     init = [_rand((I, rank), gi, device) for I in dims]
     return CpdProblem(dims, rank, X, facs, init, math.sqrt(n2 / x2), x2)
+
+
+@dataclasses.dataclass
+class HostCpdProblem:
+    dims: List[int]
+    rank: int
+    X: "np.ndarray"                 # flat float64, ColMajor
+    true_factors: list              # numpy I_k x R
+    init_factors: list              # numpy I_k x R
+    noise_rel: float
+    frob: float
+
+
+NOISE_CHUNKS = 64   # fixed, so the draw does not depend on the number of host threads
+
+
+def make_cpd_problem_host(dims: Sequence[int], rank: int, seed: int, snr_db: float,
+                          init_seed: int | None = None, equalize_columns: bool = False,
+                          threads: int | None = None) -> HostCpdProblem:
+    """The problem of ``make_cpd_problem`` drawn with numpy's PCG64 on the host, so the same
+    seed gives the same tensor on every machine (x86 or Arm, any core count): factors
+    i.i.d. U[0,1] from ``seed`` (columns equalised on request), X = [[A]] + Gaussian noise at
+    ``snr_db`` dB, the noise drawn in NOISE_CHUNKS contiguous pieces from child seeds of
+    ``SeedSequence([seed, 1])`` (filled by a thread pool; the pieces do not depend on the
+    pool size), initial factors U[0,1] from ``init_seed`` (default seed + 1)."""
+    import concurrent.futures as cf
+    import numpy as np
+    dims = [int(d) for d in dims]
+    rng = np.random.Generator(np.random.PCG64(int(seed)))
+    facs = []
+    for I in dims:
+        A = rng.random((I, rank))
+        if equalize_columns:
+            nrm = np.linalg.norm(A, axis=0, keepdims=True)
+            A = A * (nrm.mean() / nrm)
+        facs.append(A)
+    kr = facs[-1]
+    for A in reversed(facs[1:-1]):
+        kr = (kr[:, None, :] * A[None, :, :]).reshape(-1, rank)
+    total = int(np.prod(dims))
+    X = np.empty(total, dtype=np.float64)
+    Xv = X.reshape(-1, dims[0])                       # row-major (J, I0) == ColMajor (I0, J)
+    rows_per = max(1, (kr.shape[0] + 63) // 64)
+    nthr = threads or os.cpu_count() or 1
+
+    def build(j0):
+        j1 = min(kr.shape[0], j0 + rows_per)
+        np.matmul(kr[j0:j1], facs[0].T, out=Xv[j0:j1])
+        seg = Xv[j0:j1].reshape(-1)
+        return float(np.dot(seg, seg))
+
+    with cf.ThreadPoolExecutor(nthr) as ex:
+        t2 = sum(ex.map(build, range(0, kr.shape[0], rows_per)))
+    del kr
+    sigma = math.sqrt(t2 / (total * 10.0 ** (snr_db / 10.0)))
+    children = np.random.SeedSequence([int(seed), 1]).spawn(NOISE_CHUNKS)
+    step = (total + NOISE_CHUNKS - 1) // NOISE_CHUNKS
+
+    def noise(c):
+        lo, hi = c * step, min(total, (c + 1) * step)
+        if lo >= hi:
+            return 0.0, 0.0
+        g = np.random.Generator(np.random.PCG64(children[c]))
+        n = g.standard_normal(hi - lo)
+        n *= sigma
+        seg = X[lo:hi]
+        seg += n
+        return float(np.dot(n, n)), float(np.dot(seg, seg))
+
+    with cf.ThreadPoolExecutor(nthr) as ex:
+        parts = list(ex.map(noise, range(NOISE_CHUNKS)))
+    n2 = sum(p[0] for p in parts)
+    x2 = sum(p[1] for p in parts)
+    gi = np.random.Generator(np.random.PCG64(int(seed + 1 if init_seed is None else init_seed)))
+    init = [gi.random((I, rank)) for I in dims]
+    return HostCpdProblem(dims, rank, X, facs, init, math.sqrt(n2 / x2), x2)
 
 
 def factors_colmajor(A: torch.Tensor) -> torch.Tensor:
