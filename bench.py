@@ -3,28 +3,37 @@
 Workload (the 1000^3 configuration): 3-way dense tensor 1000 x 1000 x 1000, rank R=32,
 ground-truth factors i.i.d. U[0,1] with column norms equalised (seed 2), 30 dB Gaussian
 noise, initial factors U[0,1] (seed 3), nonnegativity on every mode, reference defaults
-otherwise (Nesterov delta 1e-2, acceleration and normalisation on).  Synthetic data of
-that shape stands in for user data.
+otherwise (Nesterov delta 1e-2, acceleration and normalisation on).  The tensor is drawn
+on the host with numpy's PCG64 (datagen.make_cpd_problem_host), so every machine gets the
+same values; synthetic data of that shape stands in for user data.
 
-A step is one full solve to the target: relative fit error <= noise floor + 1e-3, where the
-noise floor ||noise||/||X|| (computed in FP64 when the data is generated) is the error the
-FP64 least-squares optimum reaches up to O(R*sum(I)/prod(I)) = 1e-4 of overfit, so the
-target is "within 1e-3 of the FP64 oracle's converged fit".
+Target: relative fit error <= rel_FP64 + 1e-3, where rel_FP64 is the fit the FP64 OpenMP
+restatement of the reference's ALS (oracle/cpd_omp.c) reaches on this tensor from this
+start under the reference's own stopping rule with its default options (threshold 1e-3,
+max_iter 20: include/Cpd.hpp:339, include/PARTENSOR_basic.hpp:187-190).  That run is
+committed as tests/golden/headline_1000cubed_r32_fp64.npz (its per-sweep trace and final
+factors too) by tests/golden/make_headline_fp64.py; the bench checks the tensor's
+fingerprint against it before using it.
 
+A step is one full solve to the target.
   value    BF16 tensor storage + tcgen05 MTTKRP until the fit reaches the target, then the
            final factors' fit measured on the FP32 copy (one FP32 MTTKRP, Gram form); tensor
            already resident in HBM (seconds per solve, lower is better)
-  plain    the same solve with FP32 storage and CUDA-core MTTKRP (reported beside it)
+  fp8      the same with FP8 (e4m3, per-slab scales, dithered) storage, reported beside it
+  plain    the same solve with FP32 storage and CUDA-core MTTKRP
+  parity   |rel - rel_FP64|, factor congruence against the FP64 factors, and per sweep the
+           difference between the solve's relative error and the FP64 run's
   e2e      the one-call C ABI (ptg_cpd) from a pinned host FP64 buffer: host->device copy,
            BF16 and FP32 conversion, solve, factor download, all inside the timed region
   roofline MTTKRP launches timed live with CUDA events on their stream inside the timed
-           region; algorithmic bytes = prod(I)*2 + sum_{k != n} I_k*R*4 + I_n*R*4
-  cpu_baseline  the FP64 OpenMP restatement of the reference's CpdOpenMP (oracle/cpd_omp.c)
-           on the host cores, one full-size ALS sweep timed and scaled by the sweeps the FP64
-           algorithm needs (the FP32 plain form tracks the FP64 trajectory sweep by sweep)
+           region; algorithmic bytes = prod(I)*s + sum_{k != n} I_k*R*4 + I_n*R*4 (s = 2 for
+           BF16, 1 for FP8 plus the slab scales)
+  cpu_baseline  one full-size FP64 ALS sweep of the restatement on all host cores, times the
+           sweeps the FP64 run needs to reach the target (from its committed trace)
 
-Inputs (2 GB BF16, 4 GB FP32) are far larger than the 129 MB L2, so no flush is needed
-between steps.  ``--impl reference`` times the CPU restatement alone.
+``--impl reference`` runs that FP64 restatement to the target on the host cores and reports
+the measured wall time.  Inputs (2 GB BF16, 1 GB FP8, 4 GB FP32) are far larger than the
+129 MB L2, so no flush is needed between steps.
 """
 from __future__ import annotations
 
@@ -44,10 +53,9 @@ sys.path.insert(0, ROOT)
 DIMS = [1000, 1000, 1000]
 RANK = 32
 SEED, INIT_SEED, SNR_DB = 2, 3, 30.0
-METRIC = "time to rel. fit err <= FP64-oracle fit + 1e-3 (BF16 tcgen05 MTTKRP, fit verified on FP32 data), 1000^3 R=32 nonneg CPD-ALS"
-# Sweeps the FP64 ALS needs to reach the target on this workload (measured with the FP32
-# plain form, whose per-sweep relative error follows the FP64 oracle within 1e-4).
-SWEEPS_TO_TARGET_FP64 = None   # filled from the plain-form run when available
+METRIC = ("time to rel. fit err <= FP64-oracle fit + 1e-3 (BF16 tcgen05 MTTKRP, fit verified on FP32 data), "
+          "1000^3 R=32 nonneg CPD-ALS")
+FIXTURE = os.path.join(ROOT, "tests", "golden", "headline_1000cubed_r32_fp64.npz")
 
 
 def _peaks():
@@ -128,6 +136,44 @@ def _max_over_ranks(x, ws):
     return float(t.item())
 
 
+def _congruence(A, B):
+    """Tucker's congruence after the best column matching: per mode the absolute cosines of
+    the columns, multiplied over the modes, columns paired by linear assignment; returns
+    (mean, min) over the R pairs."""
+    import numpy as np
+    from scipy.optimize import linear_sum_assignment
+    R = A[0].shape[1]
+    C = np.ones((R, R))
+    for a, b in zip(A, B):
+        an = a / np.maximum(np.linalg.norm(a, axis=0), 1e-300)
+        bn = b / np.maximum(np.linalg.norm(b, axis=0), 1e-300)
+        C *= np.abs(an.T @ bn)
+    r, c = linear_sum_assignment(-C)
+    return float(C[r, c].mean()), float(C[r, c].min())
+
+
+def headline_problem():
+    """The seeded host tensor and the FP64 fixture; raises if the draw does not match it."""
+    import numpy as np
+    ge = __import__("__graft_entry__")
+    ge.load_package()
+    from partensor_toolbox_gb300 import datagen as dg
+    p = dg.make_cpd_problem_host(DIMS, RANK, seed=SEED, init_seed=INIT_SEED, snr_db=SNR_DB, equalize_columns=True)
+    fx = dict(np.load(FIXTURE))
+    if abs(p.frob - float(fx["frob"])) > 1e-9 * float(fx["frob"]) or \
+            not np.allclose(p.X[fx["probe_idx"]], fx["probe"], rtol=1e-12, atol=0):
+        raise RuntimeError("the seeded headline tensor does not match the FP64 fixture")
+    return p, fx
+
+
+def fp64_sweeps_to(fx, target):
+    """Sweeps the committed FP64 run needed to get below `target` (None if it never did)."""
+    for k, rel in enumerate(fx["trace"][:, 1]):
+        if rel < target:
+            return k + 1
+    return None
+
+
 def cpu_sweep_seconds(X_host_flat, dims, R, init, threads, sweeps=1):
     """One (or more) full-size FP64 ALS sweeps of the OpenMP restatement; seconds per sweep."""
     from oracle import omp
@@ -138,39 +184,36 @@ def cpu_sweep_seconds(X_host_flat, dims, R, init, threads, sweeps=1):
 
 
 def run_reference(args):
-    """CPU restatement of the reference (oracle/cpd_omp.c, FP64, all host threads)."""
+    """The FP64 OpenMP restatement of the reference's ALS (oracle/cpd_omp.c) run to the target
+    (threshold_error = rel_FP64 + 1e-3, the reference's max_iter 20) on all host cores; the
+    measured wall time is the value.  Under torchrun only rank 0 runs."""
     ws, rank = _dist()
     if rank != 0:
         return
-    import numpy as np
-    import torch
-    ge = __import__("__graft_entry__")
-    pkg = ge.load_package()
-    from partensor_toolbox_gb300 import datagen as dg
-    dev = "cuda" if torch.cuda.is_available() else "cpu"
-    p = dg.make_cpd_problem(DIMS, RANK, seed=SEED, init_seed=INIT_SEED, snr_db=SNR_DB,
-                            equalize_columns=True, device=dev)
-    Xh = p.X.cpu().numpy()
-    init = [f.cpu().numpy() for f in p.init_factors]
-    del p
+    from oracle import omp
+    p, fx = headline_problem()
+    target = float(fx["rel_fp64"]) + 1e-3
     threads = os.cpu_count() or 1
-    sweeps = args.sweeps_to_target
-    times = []
-    for _ in range(max(0, args.warmup_ref)):
-        cpu_sweep_seconds(Xh, DIMS, RANK, init, threads)
-    for _ in range(args.steps):
-        s, _ = cpu_sweep_seconds(Xh, DIMS, RANK, init, threads)
-        times.append(s)
-    per_sweep = statistics.mean(times)
-    value = per_sweep * sweeps
+    # warm-up: page the tensor in and spin up the thread pool (one sweep, untimed)
+    for _ in range(max(0, min(1, args.warmup))):
+        omp.cpd_als(p.X, DIMS, RANK, p.init_factors, max_iter=1, threshold_error=0.0, nthreads=threads)
+    t = time.perf_counter()
+    fs, st, tr = omp.cpd_als(p.X, DIMS, RANK, p.init_factors, threshold_error=target, max_iter=20, nthreads=threads)
+    value = time.perf_counter() - t
+    k = st.ao_iter
+    drift = float(abs(tr[k - 1, 1] - fx["trace"][k - 1, 1]))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_sweep * 1e3,
+            "steps": k, "warmup": args.warmup, "ms_per_step": value / k * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "cpd_als 1000x1000x1000 R=32 30dB nonneg",
-                                            "rank": RANK, "dims": DIMS, "l2": "inputs > L2"},
+            "data": "synthetic (seeded host draw: U[0,1] factors, 30 dB noise)",
+            "config": {"workload": "cpd_als 1000x1000x1000 R=32 30dB nonneg, to target", "rank": RANK,
+                       "dims": DIMS, "target_rel": target, "rel_fp64": float(fx["rel_fp64"]),
+                       "l2": "inputs > L2"},
+            "converged": bool(st.rel_costFunction < target), "final_rel_err": st.rel_costFunction,
+            "sweeps": k, "trace_vs_fixture_max_abs": drift,
             "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
-                             "sample": f"1 full-size FP64 ALS sweep per step (OpenMP restatement of "
-                                       f"CpdOpenMP, oracle/cpd_omp.c), x {sweeps} sweeps to target"},
+                             "sample": f"one FP64 solve of the OpenMP restatement of CpdOpenMP (oracle/cpd_omp.c) "
+                                       f"to the target, {k} sweeps, measured (steps = sweeps)"},
             "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -186,73 +229,100 @@ def run_ours(args):
     torch.cuda.set_device(local)
     ge = __import__("__graft_entry__")
     pkg = ge.load_package()
-    from partensor_toolbox_gb300 import datagen as dg
-    dims, R = (args.dims or DIMS) if not args.small else [200, 200, 200], RANK
-    p = dg.make_cpd_problem(dims, R, seed=SEED, init_seed=INIT_SEED, snr_db=SNR_DB, equalize_columns=True,
-                            device="cuda")
-    target = p.noise_rel + 1e-3
-    init = [f.cpu().numpy() for f in p.init_factors]
+    p, fx = headline_problem()
+    dims, R = DIMS, RANK
+    rel64 = float(fx["rel_fp64"])
+    target = rel64 + 1e-3
+    init = p.init_factors
+    Xd = torch.from_numpy(p.X).to("cuda")            # FP64 source in HBM (the tensors are built from it)
     ctx = pkg.Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
-    Xb = pkg.Tensor(ctx, (p.X.data_ptr(), dims), precision="bf16")
-    Xf = pkg.Tensor(ctx, (p.X.data_ptr(), dims), precision="f32")
+    Xb = pkg.Tensor(ctx, (Xd.data_ptr(), dims), precision="bf16")
+    X8 = pkg.Tensor(ctx, (Xd.data_ptr(), dims), precision="fp8")
+    Xf = pkg.Tensor(ctx, (Xd.data_ptr(), dims), precision="f32")
+    del Xd
+    torch.cuda.empty_cache()
     max_iter = args.max_iter
 
-    def solve(form):
-        if form == "bf16":
-            o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target, precision="bf16",
-                            verify_fp32=True)
-            return pkg.cpd_resident(ctx, Xb, R, o, init, refine=Xf)
-        o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target)
+    def solve(form, tgt=target):
+        if form in ("bf16", "fp8"):
+            o = pkg.Options(order=3, max_iter=max_iter, threshold_error=tgt, precision=form, verify_fp32=True)
+            return pkg.cpd_resident(ctx, Xb if form == "bf16" else X8, R, o, init, refine=Xf)
+        o = pkg.Options(order=3, max_iter=max_iter, threshold_error=tgt)
         return pkg.cpd_resident(ctx, Xf, R, o, init)
 
-    def timed(form, k, stats=False):
+    def timed(form, k, tgt=target):
         sts = []
         torch.cuda.synchronize()
         _barrier(ws)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        if stats:
-            ctx.enable_stats(True)
-            ctx.reset_stats()
+        ctx.enable_stats(True)
+        ctx.reset_stats()
         e0.record(stream)
         for _ in range(k):
-            sts.append(solve(form))
+            sts.append(solve(form, tgt))
         e1.record(stream)
         torch.cuda.synchronize()
         _barrier(ws)
-        st_k = ctx.stats() if stats else None
-        if stats:
-            ctx.enable_stats(False)
-        ms = e0.elapsed_time(e1) / k
-        return ms, sts, st_k
+        st_k = ctx.stats()
+        ctx.enable_stats(False)
+        return e0.elapsed_time(e1) / k, sts, st_k
 
     for _ in range(args.warmup):
         solve("bf16")
+    solve("fp8")
     solve("f32")
     clk = ClockSampler()
     clk.start()
-    ms_b, st_b, kst = timed("bf16", args.steps, stats=True)
+    ms_b, st_b, kst = timed("bf16", args.steps)
     clocks = clk.stop()
+    ms_8, st_8, kst8 = timed("fp8", max(1, args.steps_fp8))
     ms_f, st_f, _ = timed("f32", max(1, args.steps_plain))
+    # the stricter target: within 1e-3 of where the FP64 solve converges (60 sweeps), not of
+    # where the reference's default stopping rule (20 sweeps) leaves it
+    rel64_conv = float(fx["long_trace"][-1, 1])
+    strict = rel64_conv + 1e-3
+    ms_bs, st_bs, _ = timed("bf16", max(1, args.steps_plain), strict)
+    ms_fs, st_fs, _ = timed("f32", 1, strict)
     ms_b = _max_over_ranks(ms_b, ws)
+    ms_8 = _max_over_ranks(ms_8, ws)
     ms_f = _max_over_ranks(ms_f, ws)
 
-    # roofline of the dominant kernel (MTTKRP, tensor-core form)
     peak, peak_kind = _peaks()
-    launches = max(1, kst["tc_launches"])
-    per_launch_ms = kst["tc_ms"] / launches
-    bytes_per_launch = kst["tc_bytes"] / launches
-    achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
-    # DRAM bytes per launch from the ncu capture of the same kernel at 640^3 (mode 1):
-    # read 530.58 MB + write 3.66 MB, scaled by the tensor entries of this workload
-    traffic = (530.58e6 + 3.66e6) / 640 ** 3 * float(np.prod(dims))
+
+    def roofline(k, kernel, ncu_bytes, note):
+        launches = max(1, k["tc_launches"])
+        per_launch_ms = k["tc_ms"] / launches
+        bytes_per_launch = k["tc_bytes"] / launches
+        achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": ncu_bytes, "peak_kind": peak_kind, "kernel": kernel, "launches": k["tc_launches"],
+                "ms_per_launch": per_launch_ms, "bytes_per_launch": bytes_per_launch, "traffic_source": note}
+
+    # DRAM bytes per launch from ncu captures at 640^3 (mode 1), scaled by the entries of this
+    # workload: BF16 read 530.58 MB + write 3.66 MB
+    scale = float(np.prod(dims)) / 640 ** 3
+    roof_b = roofline(kst, "mttkrp_tc_kernel + tc_reduce_kernel (tcgen05 kind::f16, BF16 storage)",
+                      (530.58e6 + 3.66e6) * scale, "ncu capture at 640^3 scaled by entries (profiles/)")
+    roof_8 = roofline(kst8, "f8_colscale_kernel + mttkrp_f8_kernel + f8_reduce_kernel (tcgen05 kind::f8f6f4)",
+                      None, "no ncu capture of this build yet")
+
+    def parity(st):
+        tr = [t["rel"] for t in st.trace][: st.ao_iter]
+        ref = fx["trace"][:, 1]
+        n = min(len(tr), len(ref))
+        errs = [abs(tr[i] - float(ref[i])) for i in range(n)]
+        mean_c, min_c = _congruence(st.factors, [f.astype(np.float64) for f in fx["factors"]])
+        return {"rel_fp64": rel64, "abs_gap": abs(st.rel_costFunction - rel64), "congruence": mean_c,
+                "congruence_min": min_c, "per_sweep_abs_err": [round(e, 7) for e in errs],
+                "per_sweep_abs_err_max": max(errs) if errs else None}
 
     # end-to-end through the one-call C ABI with a pinned host FP64 buffer
     e2e = None
     if not args.no_e2e:
-        host = torch.empty(p.X.numel(), dtype=torch.float64, pin_memory=True)
-        host.copy_(p.X)
+        host = torch.empty(p.X.size, dtype=torch.float64, pin_memory=True)
+        host.numpy()[:] = p.X
         hnp = host.numpy()
         o = pkg.Options(order=3, max_iter=max_iter, threshold_error=target, precision="bf16", verify_fp32=True)
         pkg.cpd(hnp, R, o, init, dims=dims, ctx=ctx)   # warm-up
@@ -271,43 +341,49 @@ def run_ours(args):
                "calls_s": [round(x, 5) for x in ts]}
         del host
 
-    sweeps_plain = st_f[-1].ao_iter
+    sweeps64 = fp64_sweeps_to(fx, target)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        Xh = p.X.cpu().numpy()
         threads = os.cpu_count() or 1
-        s_sweep, _ = cpu_sweep_seconds(Xh, dims, R, init, threads)
-        cpu = {"value": s_sweep * sweeps_plain, "unit": "s", "cores": threads, "kind": "port",
+        s_sweep, _ = cpu_sweep_seconds(p.X, dims, R, init, threads)
+        cpu = {"value": s_sweep * sweeps64, "unit": "s", "cores": threads, "kind": "port",
                "sample": f"1 full-size FP64 ALS sweep of the OpenMP restatement of CpdOpenMP "
-                         f"(oracle/cpd_omp.c) = {s_sweep:.2f} s, x {sweeps_plain} sweeps to target "
-                         f"(the FP32 plain form's count)"}
-        del Xh
+                         f"(oracle/cpd_omp.c) = {s_sweep:.2f} s, x {sweeps64} sweeps (the FP64 run's "
+                         f"sweeps to the target, from its committed trace)"}
 
-    last_b, last_f = st_b[-1], st_f[-1]
+    last_b, last_8, last_f = st_b[-1], st_8[-1], st_f[-1]
     line = {
         "metric": METRIC, "value": ms_b / 1e3, "unit": "s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16",
-        "data": "synthetic (seeded U[0,1] factors, 30 dB Gaussian noise)",
+        "data": "synthetic (seeded host draw: U[0,1] factors, 30 dB Gaussian noise)",
         "config": {"workload": f"cpd_als {dims[0]}x{dims[1]}x{dims[2]} R={R} 30dB nonneg, to target",
-                   "rank": R, "dims": dims, "target_rel": target, "noise_floor_rel": p.noise_rel,
-                   "l2": "inputs (2 GB BF16 / 4 GB FP32) > 129 MB L2, no flush",
+                   "rank": R, "dims": dims, "target_rel": target, "rel_fp64": rel64,
+                   "fp64_sweeps_to_target": sweeps64, "noise_floor_rel": p.noise_rel,
+                   "l2": "inputs (2 GB BF16 / 1 GB FP8 / 4 GB FP32) > 129 MB L2, no flush",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "converged": bool(last_b.rel_costFunction <= target),
         "fit_measured_on": "FP32 copy of the tensor (final factors)",
         "final_rel_err": last_b.rel_costFunction,
-        "sweeps": last_b.ao_iter, "refine_sweeps": last_b.refine_sweeps_done,
-        "nesterov_iters_total": last_b.nesterov_iters_total,
-        "plain_fp32": {"value": ms_f / 1e3, "unit": "s", "sweeps": sweeps_plain,
+        "sweeps": last_b.ao_iter, "nesterov_iters_total": last_b.nesterov_iters_total,
+        "parity_fp64": parity(last_b),
+        "fp8": {"value": ms_8 / 1e3, "unit": "s", "steps": max(1, args.steps_fp8), "sweeps": last_8.ao_iter,
+                "final_rel_err": last_8.rel_costFunction, "converged": bool(last_8.rel_costFunction <= target),
+                "fit_measured_on": "FP32 copy of the tensor (final factors)", "parity_fp64": parity(last_8),
+                "roofline": roof_8},
+        "plain_fp32": {"value": ms_f / 1e3, "unit": "s", "sweeps": last_f.ao_iter,
                        "final_rel_err": last_f.rel_costFunction,
-                       "converged": bool(last_f.rel_costFunction <= target)},
+                       "converged": bool(last_f.rel_costFunction <= target), "parity_fp64": parity(last_f)},
+        "strict_target": {"target_rel": strict, "rel_fp64_converged": rel64_conv,
+                          "bf16": {"value": ms_bs / 1e3, "unit": "s", "sweeps": st_bs[-1].ao_iter,
+                                   "final_rel_err": st_bs[-1].rel_costFunction,
+                                   "converged": bool(st_bs[-1].rel_costFunction <= strict)},
+                          "plain_fp32": {"value": ms_fs / 1e3, "unit": "s", "sweeps": st_fs[-1].ao_iter,
+                                         "final_rel_err": st_fs[-1].rel_costFunction,
+                                         "converged": bool(st_fs[-1].rel_costFunction <= strict)}},
         "speedup_vs_plain_fp32": (ms_f / ms_b) if ms_b > 0 else None,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "mttkrp_tc_kernel + tc_reduce_kernel (tcgen05, BF16 storage)",
-                     "launches": kst["tc_launches"], "ms_per_launch": per_launch_ms,
-                     "bytes_per_launch": bytes_per_launch,
-                     "traffic_source": "ncu capture at 640^3 scaled by entries (profiles/)"},
+        "speedup_fp8_vs_plain_fp32": (ms_f / ms_8) if ms_8 > 0 else None,
+        "roofline": roof_b,
         "gpu_launches": kst["launches"],
         "clocks": clocks,
         "e2e": e2e,
@@ -316,6 +392,7 @@ def run_ours(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     Xb.close()
+    X8.close()
     Xf.close()
     ctx.close()
     if ws > 1:
@@ -591,15 +668,119 @@ def run_gtc(args):
                      "observed_entries_per_s": n_train * max(1, passes) / el,
                      "rel_cost": st.rel_costFunction, "heldout_rmse": rmse(st.factors)}
     floor = float(torch.sqrt(torch.mean((clean_ho - vals_ho) ** 2)))
+    cpu = None
+    if not args.no_cpu:
+        cpu = gtc_cpu_baseline(idx_tr.cpu().numpy(), vals_tr.cpu().numpy(), dims, R, init, args.gtc_c,
+                               args.gtc_epochs, args.gtc_full_iters, args.gtc_cpu_entries)
     line = {"metric": f"observed entries/s, stochastic GTC 50000x50000x5000, {total_nnz / 1e6:g}M entries, R=32, "
                       f"c={args.gtc_c:g}",
             "value": out["stochastic"]["observed_entries_per_s"], "unit": "entries/s", "n_gpus": 1,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic (uniform sample, rank-32 model, 10% noise)",
             "config": {"workload": "gtc_stochastic 50000x50000x5000", "nnz_train": n_train, "nnz_heldout": n_hold,
                        "rank": R, "lambda": 1e-3, "c_stochastic_perc": args.gtc_c},
-            "runs": out, "heldout_rmse_noise_floor": floor}
+            "runs": out, "heldout_rmse_noise_floor": floor, "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
     ctx.close()
+
+
+def run_mttkrp(args):
+    """One kernel in isolation (kernel tuning and ncu captures): mode-n MTTKRPs of a uniform
+    random tensor of --mttkrp-dims on cuda:0, timed with CUDA events on the launching stream
+    after warm-up; one JSON line per mode with the achieved bandwidth over the algorithmic
+    bytes prod(I)*s + sum_{k != n} I_k*R*4 + I_n*R*4."""
+    import numpy as np
+    import torch
+    ge = __import__("__graft_entry__")
+    pkg = ge.load_package()
+    dims, R = args.mttkrp_dims, args.mttkrp_rank
+    g = torch.Generator(device="cuda").manual_seed(0)
+    numel = int(np.prod(dims))
+    X = torch.rand(numel, generator=g, device="cuda", dtype=torch.float64)
+    ctx = pkg.Context(0)
+    ctx.set_mttkrp_impl(args.mttkrp_impl)
+    T = pkg.Tensor(ctx, (X.data_ptr(), dims), precision=args.mttkrp_precision)
+    del X
+    torch.cuda.synchronize()
+    facs = [torch.rand(I, R, generator=g, device="cuda", dtype=torch.float32) for I in dims]
+    s = torch.cuda.Stream()
+    ctx.set_stream(s.cuda_stream)
+    modes = range(len(dims)) if args.mttkrp_mode == "all" else [int(args.mttkrp_mode)]
+    esz = {"bf16": 2, "f32": 4, "fp8": 1}[args.mttkrp_precision]
+    peak, peak_kind = _peaks()
+    for mode in modes:
+        out = torch.empty(dims[mode], R, device="cuda")
+        ptrs = [f.data_ptr() for f in facs]
+        for _ in range(args.warmup):
+            pkg.mttkrp(ctx, T, ptrs, R, mode, out.data_ptr())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(args.steps):
+            pkg.mttkrp(ctx, T, ptrs, R, mode, out.data_ptr())
+        e1.record(s)
+        e1.synchronize()
+        ctx.synchronize()
+        ms = e0.elapsed_time(e1) / max(1, args.steps)
+        nbytes = numel * esz + sum(I * R * 4 for k, I in enumerate(dims) if k != mode) + dims[mode] * R * 4
+        if args.mttkrp_precision == "fp8":
+            nbytes += dims[-1] * 4
+        print(json.dumps({"workload": "mttkrp", "mode": mode, "dims": dims, "rank": R,
+                          "precision": args.mttkrp_precision, "impl": args.mttkrp_impl, "ms": ms,
+                          "GBps": nbytes / ms / 1e6, "frac": nbytes / ms / 1e6 / peak, "peak_kind": peak_kind,
+                          "TFLOPs": 2.0 * numel * R / ms / 1e9}), flush=True)
+    T.close()
+    ctx.close()
+
+
+def gtc_cpu_baseline(idx, vals, dims, R, init, c, epochs, full_iters, sample_entries):
+    """The FP64 OpenMP restatement of the reference's GTC row solvers (oracle/gtc_omp.c) on
+    all host cores, timed on a bounded sample of the same workload: for each mode the rows
+    i_n < S_n (S_n = I_n * sample_entries / nnz, so each sample holds about sample_entries
+    observed entries) get one factor update, the stochastic block solver and the local_L
+    solver, from the initial factors.  A row's work is proportional to its entries, so a
+    mode's time scales by nnz / (the sample's entries); the stochastic run then takes
+    epochs * (floor(nnz / (blocksize_0 * I_0)) + 1) outer iterations
+    (include/GtcStochastic.hpp:431,452-465), the full run full_iters.  Cost evaluations (one
+    pass over the entries per epoch or iteration) are not counted."""
+    import numpy as np
+    from oracle import omp
+    N, nnz = len(dims), idx.shape[1]
+    threads = os.cpu_count() or 1
+    frac = min(1.0, sample_entries / nnz)
+    fac = [np.asarray(f, dtype=np.float64) for f in init]
+    t_sto = t_full = 0.0
+    used = []
+    for n in range(N):
+        S = max(1, int(dims[n] * frac))
+        sel = np.nonzero(idx[n] < S)[0]
+        others = [k for k in range(N) if k != n]
+        lin = np.zeros(sel.size, dtype=np.int64)
+        stride = 1
+        for k in others:
+            lin += idx[k][sel].astype(np.int64) * stride
+            stride *= dims[k]
+        key = idx[n][sel].astype(np.int64) * stride + lin
+        order = sel[np.argsort(key, kind="stable")]
+        ptr = np.zeros(S + 1, dtype=np.int64)
+        ptr[1:] = np.cumsum(np.bincount(idx[n][order], minlength=S))
+        other = np.stack([idx[k][order] for k in others], axis=1).astype(np.int32)
+        v = vals[order].astype(np.float64)
+        scale = nnz / max(1, order.size)
+        t = time.perf_counter()
+        omp.gtc_rows(ptr, other, v, fac, n, True, c, 20, 1e-3, seed=0, outer=1, nthreads=threads)
+        t_sto += (time.perf_counter() - t) * scale
+        t = time.perf_counter()
+        omp.gtc_rows(ptr, other, v, fac, n, False, c, 20, 1e-3, nthreads=threads)
+        t_full += (time.perf_counter() - t) * scale
+        used.append(int(order.size))
+    block0 = int(c * nnz / dims[0]) + 1
+    outer = epochs * (int(nnz / (block0 * dims[0])) + 1)
+    sto_s, full_s = t_sto * outer, t_full * full_iters
+    return {"value": nnz * epochs / sto_s, "unit": "entries/s", "cores": threads, "kind": "port",
+            "seconds": sto_s, "full": {"value": nnz * full_iters / full_s, "unit": "entries/s", "seconds": full_s},
+            "sample": f"one factor update per mode on the rows holding {used} of the {nnz} entries, FP64 OpenMP "
+                      f"restatement of the reference's GTC row solvers (oracle/gtc_omp.c); scaled by entries to "
+                      f"a full update, x {outer} outer iterations ({epochs} epochs) for the stochastic run and "
+                      f"x {full_iters} for the full one; cost passes not counted"}
 
 
 def dataclasses_replace(o, **kw):
@@ -614,21 +795,27 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--steps-plain", type=int, default=2)
+    ap.add_argument("--steps-fp8", type=int, default=5)
     ap.add_argument("--steps-e2e", type=int, default=5)
     ap.add_argument("--max-iter", type=int, default=200)
-    ap.add_argument("--small", action="store_true", help="200^3 smoke configuration")
-    ap.add_argument("--dims", type=int, nargs=3, default=None, help="override the tensor shape (profiling)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--warmup-ref", type=int, default=0)
-    ap.add_argument("--sweeps-to-target", type=int, default=20)
-    ap.add_argument("--workload", default="cpd-1000", choices=["cpd-1000", "fmri-batch", "dimtree-160", "gtc-sparse"],
+    ap.add_argument("--workload", default="cpd-1000",
+                    choices=["cpd-1000", "fmri-batch", "dimtree-160", "gtc-sparse", "mttkrp"],
                     help="cpd-1000: the headline 1000^3 solve; fmri-batch: 256 small CPDs in one call; "
-                         "dimtree-160: 160^4 R=64 cpdDimTree; gtc-sparse: 200M-entry stochastic completion")
+                         "dimtree-160: 160^4 R=64 cpdDimTree; gtc-sparse: 200M-entry stochastic completion; "
+                         "mttkrp: one MTTKRP kernel in isolation (tuning, ncu captures)")
+    ap.add_argument("--mttkrp-dims", type=int, nargs="+", default=[640, 640, 640])
+    ap.add_argument("--mttkrp-rank", type=int, default=32)
+    ap.add_argument("--mttkrp-precision", default="bf16", choices=["bf16", "f32", "fp8"])
+    ap.add_argument("--mttkrp-impl", default="auto", choices=["auto", "cuda_cores", "tensor_cores"])
+    ap.add_argument("--mttkrp-mode", default="all")
     ap.add_argument("--gtc-nnz", type=float, default=200e6)
     ap.add_argument("--gtc-epochs", type=int, default=2, help="stochastic GTC epochs (its max_iter)")
     ap.add_argument("--gtc-full-iters", type=int, default=2)
     ap.add_argument("--gtc-c", type=float, default=0.01, help="sampled fraction of each row per inner step")
+    ap.add_argument("--gtc-cpu-entries", type=float, default=4e6, help="observed entries per mode the CPU baseline solves")
     ap.add_argument("--batch-sample", type=int, default=32, help="instances the CPU baseline solves")
     args = ap.parse_args()
     if args.workload == "fmri-batch":
@@ -637,6 +824,8 @@ def main():
         run_dimtree(args)
     elif args.workload == "gtc-sparse":
         run_gtc(args)
+    elif args.workload == "mttkrp":
+        run_mttkrp(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -36,7 +36,13 @@ typedef enum {
   PTG_ERR_NUMERIC = 6      /* NaN/Inf detected in an input or a result */
 } ptg_status;
 
-typedef enum { PTG_F32 = 0, PTG_BF16 = 1 } ptg_dtype;
+/* Storage of a dense tensor in HBM.  PTG_FP8E4M3: one byte per entry, the e4m3 code of
+ * x / scale_s, where s is the entry's index in the last mode (its slab) and scale_s = 2^k the
+ * smallest power of two with max_slab |x| <= 448 * 2^k; rounding is stochastic (up with
+ * probability equal to the distance from the lower e4m3 neighbour, from a hash of the
+ * entry's position), so the stored copy is unbiased.  The ALS cost on FP8 storage uses the
+ * FP64 source norm, which makes it an unbiased estimate of the cost on the data. */
+typedef enum { PTG_F32 = 0, PTG_BF16 = 1, PTG_FP8E4M3 = 2 } ptg_dtype;
 
 /* Constraint values of include/Constants.hpp:49-57. */
 typedef enum {
@@ -78,7 +84,14 @@ typedef enum {
                              schedules it, else 8), or 2, 4, 8, 16 */,
   PTG_OPT_GTC_ROWS = 3 /* sparse row solver of the nonnegative GTC modes: 0 auto (one warp per
                           row for rank <= 32, else one CTA per row), 1 one CTA per row; both
-                          give the same bits */
+                          give the same bits */,
+  PTG_OPT_SPIN_LIMIT = 4 /* polls of every bounded wait in the tensor-core MTTKRP kernels before
+                            they give up with PTG_ERR_TIMEOUT: -1 the default (2^26), 0 give up
+                            at once, before any copy or MMA is issued (a test of the failure
+                            path) */,
+  PTG_OPT_ALLOC_LIMIT = 5 /* largest single device allocation (bytes) this context may make; a
+                             larger request fails with PTG_ERR_OOM as cudaMalloc would and
+                             leaves the context usable (0: no limit) */
 } ptg_option;
 int ptg_ctx_set_option(ptg_ctx *ctx, int option, long long value);
 
@@ -108,13 +121,18 @@ int ptg_ctx_reset_stats(ptg_ctx *ctx);
  * buffer with prod(dims) entries, on the host (src_on_device = 0) or on the device.
  * Replaces the host Matricization copies of include/CUDA/CpdCUDA.hpp:302-306: the
  * tensor is stored once, in its natural order, with mode 0 padded to a multiple of 8
- * (pads are zero).  ||X||^2 (include/TensorOperations.hpp:144-149) is computed in FP64
+ * entries (16 for FP8 storage; pads are zero).  ||X||^2 (include/TensorOperations.hpp:144-149) is computed in FP64
  * from the FP64 source during the upload. */
 int ptg_tensor_create(ptg_ctx *ctx, int order, const int64_t *dims, ptg_dtype dtype,
                       const double *src, int src_on_device, ptg_tensor **out);
 int ptg_tensor_destroy(ptg_tensor *t);
 /* frob64: ||X||^2 of the FP64 source; frob_stored: ||X||^2 of the stored (rounded) copy. */
 int ptg_tensor_norms(const ptg_tensor *t, double *frob64, double *frob_stored);
+/* The stored copy, for inspection (no counterpart in the reference, which keeps the FP64
+ * tensor itself): device address of the entries (ColMajor, mode 0 padded to *padded_dim0),
+ * and for FP8 storage the device address of the slab scales (one float per index of the
+ * last mode; NULL for the other types).  Any output pointer may be NULL. */
+int ptg_tensor_storage(const ptg_tensor *t, const void **data, int64_t *padded_dim0, const float **slab_scales);
 
 /* Mode-n MTTKRP, M = X_(n) * KhatriRao_{k != n}(A_k).  Replaces mttkrp
  * (include/MTTKRP.hpp:60-69, 102-225) and hybrid_batched_mttkrp
@@ -166,10 +184,19 @@ typedef struct {
                            trained warm_train_steps Adam steps and used from sweep n+1;
                            0: use the network as it is from sweep 1 */
   int warm_train_steps;
-  int verify_fp32;      /* 1: after a main loop on BF16 storage with no refinement sweeps, the
-                           reported cost is that of the final factors on an FP32 copy of the
-                           tensor (one more MTTKRP); ptg_cpd_als needs `refine`, ptg_cpd and
-                           ptg_cpd_dimtree make the copy from the same upload */
+  int verify_fp32;      /* 1: after a main loop on BF16 or FP8 storage with no refinement
+                           sweeps, the reported cost is that of the final factors on an FP32
+                           copy of the tensor (one more MTTKRP); ptg_cpd_als needs `refine`,
+                           ptg_cpd and ptg_cpd_dimtree make the copy from the same upload */
+  /* partensor::Options::writeToFile / final_factors_paths (include/PARTENSOR_basic.hpp:
+   * 326-333, include/Cpd.hpp:112-122,340-342): when write_to_file is 1, the final factors
+   * are written when the loop stops, factor k as I_k x R FP64 in row-major order (the
+   * reference writes the transpose of the ColMajor matrix, include/ReadWrite.hpp:100-130)
+   * to final_factors_paths[k], or to "final_<k>.bin" where that entry is NULL.  A file
+   * that cannot be written makes the call return PTG_ERR_INVALID after the factors have
+   * been returned (the reference prints to stderr and continues). */
+  int write_to_file;
+  const char *final_factors_paths[PTG_MAX_ORDER];
 } ptg_cpd_options;
 
 /* Fill *o with the reference defaults (include/PARTENSOR_basic.hpp:176-218). */

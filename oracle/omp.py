@@ -1,5 +1,7 @@
-"""ctypes wrapper of oracle/cpd_omp.c -- TEST INFRASTRUCTURE ONLY (CPU baseline and a
-second restatement of the reference's CpdOpenMP driver, include/CpdOpenMP.hpp:266-329)."""
+"""ctypes wrapper of oracle/cpd_omp.c and oracle/gtc_omp.c -- TEST INFRASTRUCTURE ONLY (CPU
+baselines and second restatements of the reference's CpdOpenMP driver,
+include/CpdOpenMP.hpp:266-329, and of its OpenMP GTC row solvers,
+include/NesterovMNLS.hpp:553-663,878-976)."""
 from __future__ import annotations
 
 import ctypes
@@ -29,11 +31,12 @@ class Status(ctypes.Structure):
 
 
 def build(force: bool = False) -> str:
-    """Compile oracle/cpd_omp.c with gcc (portable flags: it also builds on the Arm host)."""
-    src = os.path.join(HERE, "cpd_omp.c")
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    """Compile oracle/cpd_omp.c and oracle/gtc_omp.c with gcc (portable flags: they also
+    build on the Arm host)."""
+    srcs = [os.path.join(HERE, "cpd_omp.c"), os.path.join(HERE, "gtc_omp.c")]
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(s) for s in srcs):
         os.makedirs(os.path.dirname(LIB), exist_ok=True)
-        subprocess.check_call(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-o", LIB, src, "-lm"])
+        subprocess.check_call(["gcc", "-O3", "-fopenmp", "-fPIC", "-shared", "-o", LIB, *srcs, "-lm"])
     return LIB
 
 
@@ -51,6 +54,11 @@ def lib():
                                       ctypes.POINTER(Options), ctypes.POINTER(dp),
                                       ctypes.POINTER(Status), dp]
         _lib.ptgo_cpd_als.restype = ctypes.c_int
+        _lib.ptgo_gtc_rows.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.c_int64, ctypes.POINTER(ctypes.c_int32), dp, ctypes.POINTER(dp),
+                                       ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
+        _lib.ptgo_gtc_rows.restype = ctypes.c_int
     return _lib
 
 
@@ -91,3 +99,23 @@ def cpd_als(X_flat: np.ndarray, dims, R: int, factors_init, constraints=None,
     X = np.ascontiguousarray(X_flat, dtype=np.float64)
     lib().ptgo_cpd_als(N, d, _dp(X), R, ctypes.byref(o), arr, ctypes.byref(st), _dp(trace))
     return fs, st, trace.reshape(-1, 3)[: st.ao_iter]
+
+
+def gtc_rows(ptr: np.ndarray, other: np.ndarray, vals: np.ndarray, factors, mode: int, stochastic: bool,
+             c: float, max_inner: int, lam: float, seed: int = 0, outer: int = 1, nthreads: int = 0):
+    """One GTC update of factor `mode` over the rows of a column-compressed matricisation
+    (ptr [nrows + 1], other [nnz, N - 1] int32, vals [nnz]); factors are I_k x R arrays, the
+    updated rows of factors[mode] are returned (the others are not changed)."""
+    N = len(factors)
+    R = factors[0].shape[1]
+    fs = [np.ascontiguousarray(f, dtype=np.float64).copy() for f in factors]
+    arr = (ctypes.POINTER(ctypes.c_double) * N)(*[_dp(f) for f in fs])
+    p = np.ascontiguousarray(ptr, dtype=np.int64)
+    o = np.ascontiguousarray(other, dtype=np.int32)
+    v = np.ascontiguousarray(vals, dtype=np.float64)
+    rc = lib().ptgo_gtc_rows(N, R, mode, p.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), len(p) - 1,
+                             o.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _dp(v), arr, int(stochastic),
+                             float(c), int(max_inner), float(lam), int(seed), int(outer), int(nthreads))
+    if rc != 0:
+        raise RuntimeError("ptgo_gtc_rows failed")
+    return fs[mode][: len(p) - 1]

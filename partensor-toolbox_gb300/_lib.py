@@ -12,17 +12,19 @@ LIB_PATH = os.path.join(HERE, "libptg.so")
 MAX_ORDER = 8
 
 PTG_OK, PTG_ERR_INVALID, PTG_ERR_CUDA, PTG_ERR_OOM, PTG_ERR_UNSUPPORTED, PTG_ERR_TIMEOUT, PTG_ERR_NUMERIC = range(7)
-PTG_F32, PTG_BF16 = 0, 1
+PTG_F32, PTG_BF16, PTG_FP8E4M3 = 0, 1, 2
 PTG_OPT_MTTKRP_IMPL = 1
 PTG_OPT_NNLS_CLUSTER = 2
 PTG_OPT_GTC_ROWS = 3
+PTG_OPT_SPIN_LIMIT = 4
+PTG_OPT_ALLOC_LIMIT = 5
 MTTKRP_IMPLS = {"auto": 0, "cuda_cores": 1, "tensor_cores": 2}
 
 # every symbol include/ptg.h declares
 EXPORTS = [
     "ptg_last_error", "ptg_version", "ptg_ctx_create", "ptg_ctx_destroy", "ptg_ctx_set_stream",
     "ptg_ctx_synchronize", "ptg_ctx_set_option", "ptg_ctx_enable_stats", "ptg_ctx_get_stats", "ptg_ctx_reset_stats",
-    "ptg_tensor_create", "ptg_tensor_destroy", "ptg_tensor_norms",
+    "ptg_tensor_create", "ptg_tensor_destroy", "ptg_tensor_norms", "ptg_tensor_storage",
     "ptg_mttkrp", "ptg_cpd_default_options", "ptg_cpd_als", "ptg_cpd",
     "ptg_cpd_dimtree_als", "ptg_cpd_dimtree", "ptg_mttkrp_noalloc", "ptg_cpd_batched",
     "ptg_tensor_create_file", "ptg_cpd_file", "ptg_cpd_dimtree_file",
@@ -40,7 +42,8 @@ class CpdOptions(ctypes.Structure):
                 ("refine_sweeps", ctypes.c_int), ("warm_start", ctypes.c_int),
                 ("cost_every_sweep", ctypes.c_int), ("warm_model", ctypes.c_void_p),
                 ("warm_log_sweeps", ctypes.c_int), ("warm_train_steps", ctypes.c_int),
-                ("verify_fp32", ctypes.c_int)]
+                ("verify_fp32", ctypes.c_int), ("write_to_file", ctypes.c_int),
+                ("final_factors_paths", ctypes.c_char_p * MAX_ORDER)]
 
 
 class CpdResult(ctypes.Structure):
@@ -117,6 +120,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.ptg_tensor_create.argtypes = [vp, ctypes.c_int, i64p, ctypes.c_int, dp, ctypes.c_int, ctypes.POINTER(vp)]
     lib.ptg_tensor_destroy.argtypes = [vp]
     lib.ptg_tensor_norms.argtypes = [vp, dp, dp]
+    lib.ptg_tensor_storage.argtypes = [vp, ctypes.POINTER(vp), i64p, ctypes.POINTER(vp)]
     lib.ptg_mttkrp.argtypes = [vp, vp, ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int, vp]
     lib.ptg_cpd_default_options.argtypes = [ctypes.c_int, ctypes.POINTER(CpdOptions)]
     lib.ptg_cpd_default_options.restype = None

@@ -10,6 +10,7 @@ are I_k x R float64.  All compute runs in libptg on the GPU; there is no CPU pat
 from __future__ import annotations
 
 import ctypes
+import os
 import dataclasses
 from typing import List, Optional, Sequence
 
@@ -19,7 +20,7 @@ from . import _lib
 from ._lib import CpdInstance, CpdOptions, CpdResult, SweepTrace, check
 
 UNCONSTRAINED, NONNEGATIVITY, ORTHOGONALITY, SPARSITY, CONSTANT = 0, 1, 2, 3, 4
-DTYPES = {"f32": _lib.PTG_F32, "fp32": _lib.PTG_F32, "bf16": _lib.PTG_BF16}
+DTYPES = {"f32": _lib.PTG_F32, "fp32": _lib.PTG_F32, "bf16": _lib.PTG_BF16, "fp8": _lib.PTG_FP8E4M3}
 
 
 @dataclasses.dataclass
@@ -35,14 +36,16 @@ class Options:
     accel_fail: int = 0
     acceleration: bool = True
     normalization: bool = True
+    writeToFile: bool = False     # write the final factors (row-major FP64) when the loop stops
+    final_factors_paths: Optional[List[str]] = None   # default "final_<k>.bin"
     # GB300 extensions
-    precision: str = "f32"        # storage of the tensor in HBM: "f32" or "bf16"
-    refine_sweeps: int = 0        # FP32 sweeps after the main loop (bf16 storage only)
+    precision: str = "f32"        # storage of the tensor in HBM: "f32", "bf16" or "fp8" (e4m3, slab scales)
+    refine_sweeps: int = 0        # FP32 sweeps after the main loop (bf16 / fp8 storage)
     warm_start: bool = False      # learned warm start of the NNLS rows (needs warm_model)
     warm_model: object = None     # a WarmStartModel
     warm_log_sweeps: int = 5      # sweeps that log training pairs before the network is trained
     warm_train_steps: int = 200
-    verify_fp32: bool = False     # report the final cost on an FP32 copy (bf16 storage, no refinement)
+    verify_fp32: bool = False     # report the final cost on an FP32 copy (bf16 / fp8 storage, no refinement)
 
     def __post_init__(self):
         if self.constraints is None:
@@ -67,6 +70,11 @@ class Options:
         o.warm_log_sweeps = int(self.warm_log_sweeps)
         o.warm_train_steps = int(self.warm_train_steps)
         o.verify_fp32 = int(bool(self.verify_fp32))
+        o.write_to_file = int(bool(self.writeToFile))
+        # the encoded paths must outlive the call that reads the struct: kept on the struct
+        o._paths = [os.fsencode(p) if p is not None else None for p in (self.final_factors_paths or [])]
+        for k, p in enumerate(o._paths[:_lib.MAX_ORDER]):
+            o.final_factors_paths[k] = p
         return o
 
 
@@ -113,6 +121,16 @@ class Context:
         """Row solver of the sparse completion's nonnegative modes: "auto" (one warp per row
         for rank <= 32) or "cta" (one CTA per row); both give the same bits."""
         check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_GTC_ROWS, {"auto": 0, "cta": 1}[solver]))
+
+    def set_spin_limit(self, polls: int):
+        """Polls of the tensor-core kernels' bounded waits before they give up with
+        PTG_ERR_TIMEOUT: -1 the default, 0 at once (exercises the failure path)."""
+        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_SPIN_LIMIT, int(polls)))
+
+    def set_alloc_limit(self, nbytes: int):
+        """Largest single device allocation the context may make (0: no limit); a larger
+        one fails with PTG_ERR_OOM."""
+        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_ALLOC_LIMIT, int(nbytes)))
 
     def enable_stats(self, on: bool = True):
         check(self._lib.ptg_ctx_enable_stats(self.handle, int(on)))
@@ -190,6 +208,14 @@ class Tensor:
         a, b = ctypes.c_double(), ctypes.c_double()
         check(self._lib.ptg_tensor_norms(self.handle, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def storage(self):
+        """(device address of the stored entries, padded mode-0 extent, device address of the
+        FP8 slab scales or None)"""
+        d, s = ctypes.c_void_p(), ctypes.c_void_p()
+        p0 = ctypes.c_int64()
+        check(self._lib.ptg_tensor_storage(self.handle, ctypes.byref(d), ctypes.byref(p0), ctypes.byref(s)))
+        return d.value, p0.value, s.value
 
     def close(self):
         if getattr(self, "handle", None):

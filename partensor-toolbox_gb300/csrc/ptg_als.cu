@@ -40,7 +40,8 @@ struct AlsBuffers {
   unsigned *cticket = nullptr;    // and its ticket (zero between launches)
   void *base = nullptr;
 
-  int alloc(const int64_t *dims, int order, int rank, int64_t rows_left = 0, int64_t rows_right = 0) {
+  int alloc(const ptg_ctx *ctx, const int64_t *dims, int order, int rank, int64_t rows_left = 0,
+            int64_t rows_right = 0) {
     N = order;
     R = rank;
     size_t off = 0;
@@ -74,10 +75,10 @@ struct AlsBuffers {
     const size_t o_W = take(sizeof(double) * R * R);
     const size_t o_cp = take(sizeof(double) * kCostPartials);
     const size_t o_ct = take(sizeof(unsigned));
-    cudaError_t e = cudaMalloc(&base, off);
-    if (e != cudaSuccess) {
+    const int rc = ctx_malloc(ctx, &base, off, "ALS buffers");
+    if (rc != PTG_OK) {
       base = nullptr;
-      return cuda_error(e, "cudaMalloc(ALS buffers)", __FILE__, __LINE__);
+      return rc;
     }
     char *b = (char *)base;
     for (int k = 0; k < N; ++k) {
@@ -97,7 +98,7 @@ struct AlsBuffers {
     W = (double *)(b + o_W);
     cpart = (double *)(b + o_cp);
     cticket = (unsigned *)(b + o_ct);
-    e = cudaMemset(cticket, 0, sizeof(unsigned));
+    const cudaError_t e = cudaMemset(cticket, 0, sizeof(unsigned));
     if (e != cudaSuccess) return cuda_error(e, "cudaMemset(ALS ticket)", __FILE__, __LINE__);
     return PTG_OK;
   }
@@ -376,6 +377,27 @@ void ptg_cpd_default_options(int order, ptg_cpd_options *o) {
 
 }  // extern "C"
 
+// writeFactorsToFile, include/Cpd.hpp:112-122: factor k (I_k x R ColMajor FP64) written as
+// its transpose's storage, i.e. row-major, to final_factors_paths[k] ("final_<k>.bin" when
+// NULL, the reference's default, include/PARTENSOR_basic.hpp:330-333).
+static int write_final_factors(const ptg_cpd_options &opt, const int64_t *dims, int N, int rank,
+                               double *const *factors) {
+  std::vector<double> row;
+  for (int k = 0; k < N; ++k) {
+    const std::string path = opt.final_factors_paths[k] ? std::string(opt.final_factors_paths[k])
+                                                        : "final_" + std::to_string(k) + ".bin";
+    const int64_t I = dims[k];
+    row.resize((size_t)I * rank);
+    for (int64_t i = 0; i < I; ++i)
+      for (int r = 0; r < rank; ++r) row[(size_t)i * rank + r] = factors[k][i + I * r];
+    FILE *fp = std::fopen(path.c_str(), "wb");
+    const bool ok = fp && std::fwrite(row.data(), sizeof(double), row.size(), fp) == row.size();
+    if (fp && std::fclose(fp) != 0) return set_error(PTG_ERR_INVALID, "cannot write " + path);
+    if (!ok) return set_error(PTG_ERR_INVALID, "cannot write " + path);
+  }
+  return PTG_OK;
+}
+
 static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *refine, int rank,
                         const ptg_cpd_options *opts_in, const double *const *init_factors,
                         double *const *out_factors, ptg_cpd_result *result, ptg_sweep_trace *trace,
@@ -398,7 +420,7 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
   Runner run{ctx, &opt};
   run.t0 = std::chrono::steady_clock::now();
   run.dimtree = dimtree;
-  PTG_TRY(run.b.alloc(X->dims, N, rank, dimtree ? node_rows(X, true) : 0, dimtree ? node_rows(X, false) : 0));
+  PTG_TRY(run.b.alloc(ctx, X->dims, N, rank, dimtree ? node_rows(X, true) : 0, dimtree ? node_rows(X, false) : 0));
   AlsBuffers &b = run.b;
   cudaStream_t S = ctx->stream;
 
@@ -430,7 +452,7 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
       }
 
   const ptg_tensor *Xa = X;
-  double frob = Xa->frob_stored;
+  double frob = cost_norm(Xa);
   double f = 0.0, rel = 0.0;
   PTG_TRY(run.point_cost(Xa, frob, b.fac, b.gram, &f));
   int ao_iter = 0, ntrace = 0;
@@ -568,7 +590,7 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
   int refined = 0;
   if (refine && opt.refine_sweeps > 0) {
     Xa = refine;
-    frob = Xa->frob_stored;
+    frob = cost_norm(Xa);
     for (int n = 0; n < N; ++n) run.warm[n] = WarmArgs();
     for (; refined < opt.refine_sweeps; ++refined) {
       PTG_TRY(run.sweep(Xa, frob, &f, iters));
@@ -590,7 +612,7 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
   // the cost of the final factors on the FP32 copy (one MTTKRP in the Gram form)
   if (refine && refined == 0 && opt.verify_fp32) {
     Xa = refine;
-    frob = Xa->frob_stored;
+    frob = cost_norm(Xa);
     PTG_TRY(run.point_cost(Xa, frob, b.fac, b.gram, &f));
     rel = f / std::sqrt(frob);
   }
@@ -614,6 +636,7 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
     result->nesterov_iters_total = inner_total;
     result->seconds_total = run.elapsed();
   }
+  if (opt.write_to_file) PTG_TRY(write_final_factors(opt, X->dims, N, rank, out_factors));
   return PTG_OK;
 }
 

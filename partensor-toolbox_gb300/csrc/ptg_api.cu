@@ -31,6 +31,10 @@ int DevBuf::ensure(size_t need) {
     bytes = 0;
   }
   size_t sz = std::max(need, (size_t)1 << 20);
+  if (limit && *limit > 0 && sz > (size_t)*limit) {
+    if (need > (size_t)*limit) return set_error(PTG_ERR_OOM, "device allocation above the context's limit");
+    sz = need;
+  }
   cudaError_t e = cudaMalloc(&ptr, sz);
   if (e != cudaSuccess) {
     ptr = nullptr;
@@ -38,6 +42,22 @@ int DevBuf::ensure(size_t need) {
   }
   bytes = sz;
   return PTG_OK;
+}
+
+int ctx_malloc(const ptg_ctx *ctx, void **p, size_t bytes, const char *what) {
+  *p = nullptr;
+  if (ctx && ctx->alloc_limit > 0 && bytes > (size_t)ctx->alloc_limit)
+    return set_error(PTG_ERR_OOM, std::string("cudaMalloc(") + what + "): above the context's allocation limit");
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return cuda_error(e, what, __FILE__, __LINE__);
+  }
+  return PTG_OK;
+}
+
+uint32_t spin_limit(const ptg_ctx *ctx) {
+  return ctx->spin_limit < 0 ? kDefaultSpinLimit : (uint32_t)ctx->spin_limit;
 }
 
 void DevBuf::release() {
@@ -245,6 +265,7 @@ int ptg_ctx_create(int device, ptg_ctx **out) {
     return cuda_error(e, "ptg_ctx_create", __FILE__, __LINE__);
   }
   c->stream = c->own_stream;
+  c->scratch.limit = c->cache_x.limit = c->cache_xr.limit = &c->alloc_limit;
   *out = c;
   return PTG_OK;
 }
@@ -257,6 +278,7 @@ int ptg_ctx_destroy(ptg_ctx *c) {
   stats_resolve(c);
   for (cudaEvent_t e : c->stats.pool) cudaEventDestroy(e);
   if (c->dev_err) cudaFree(c->dev_err);
+  if (c->f8_work) cudaFree(c->f8_work);
   if (c->pinned) cudaFreeHost(c->pinned);
   c->cache_x.release();
   c->cache_xr.release();
@@ -299,6 +321,14 @@ int ptg_ctx_set_option(ptg_ctx *c, int option, long long value) {
     case PTG_OPT_GTC_ROWS:
       if (value != 0 && value != 1) return set_error(PTG_ERR_INVALID, "GTC row solver must be 0 (auto) or 1");
       c->gtc_rows = (int)value;
+      return PTG_OK;
+    case PTG_OPT_SPIN_LIMIT:
+      if (value < -1 || value > 0xffffffffLL) return set_error(PTG_ERR_INVALID, "spin limit must be -1 or in [0, 2^32)");
+      c->spin_limit = value;
+      return PTG_OK;
+    case PTG_OPT_ALLOC_LIMIT:
+      if (value < 0) return set_error(PTG_ERR_INVALID, "allocation limit must be >= 0");
+      c->alloc_limit = value;
       return PTG_OK;
     default:
       return set_error(PTG_ERR_INVALID, "unknown option");
@@ -366,7 +396,8 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
   }
   if (order < 2 || order > PTG_MAX_ORDER)
     return set_error(PTG_ERR_UNSUPPORTED, "tensor order must be in [2, 8]");
-  if (dtype != PTG_F32 && dtype != PTG_BF16) return set_error(PTG_ERR_UNSUPPORTED, "dtype");
+  if (dtype != PTG_F32 && dtype != PTG_BF16 && dtype != PTG_FP8E4M3) return set_error(PTG_ERR_UNSUPPORTED, "dtype");
+  const bool fp8 = dtype == PTG_FP8E4M3;
   int64_t numel = 1;
   for (int k = 0; k < order; ++k) {
     if (dims[k] < 1 || dims[k] > 0x7fffffffLL)
@@ -377,23 +408,38 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
   ptg_tensor *t = new ptg_tensor();
   t->order = order;
   for (int k = 0; k < order; ++k) t->dims[k] = dims[k];
-  t->pdim0 = (dims[0] + 7) / 8 * 8;
+  // rows of 16 bytes: TMA copies start on 16-byte boundaries
+  const int64_t pad = fp8 ? 16 : 8;
+  t->pdim0 = (dims[0] + pad - 1) / pad * pad;
   t->numel_padded = numel / dims[0] * t->pdim0;
   t->dtype = dtype;
   t->device = c->device;
-  const size_t esz = dtype == PTG_F32 ? 4 : 2;
-  cudaError_t e = cudaSuccess;
+  const size_t esz = dtype == PTG_F32 ? 4 : dtype == PTG_BF16 ? 2 : 1;
+  // FP8: the codes, then the slab scales and the slab maxima in the same allocation
+  const int64_t nslab = dims[order - 1];
+  const size_t code_bytes = ((size_t)t->numel_padded * esz + 255) / 256 * 256;
+  const size_t scale_bytes = fp8 ? ((size_t)nslab * sizeof(float) + 255) / 256 * 256 : 0;
+  const size_t total_bytes = code_bytes + scale_bytes + (fp8 ? (size_t)nslab * sizeof(unsigned long long) : 0);
   if (storage) {   // a context-owned buffer, kept for the next call
-    const int rs = storage->ensure((size_t)t->numel_padded * esz);
+    const int rs = storage->ensure(total_bytes);
     if (rs != PTG_OK) {
       delete t;
       return rs;
     }
     t->data = storage->ptr;
     t->owns = false;
-  } else if ((e = cudaMalloc(&t->data, (size_t)t->numel_padded * esz)) != cudaSuccess) {
-    delete t;
-    return cuda_error(e, "cudaMalloc(tensor)", __FILE__, __LINE__);
+  } else {
+    const int rs = ctx_malloc(c, &t->data, total_bytes, "tensor");
+    if (rs != PTG_OK) {
+      delete t;
+      return rs;
+    }
+  }
+  cudaError_t e = cudaSuccess;
+  unsigned long long *slab_bits = nullptr;
+  if (fp8) {
+    t->f8_scales = (float *)((char *)t->data + code_bytes);
+    slab_bits = (unsigned long long *)((char *)t->data + code_bytes + scale_bytes);
   }
   // the optional FP32 copy, written by the same pass
   ptg_tensor *t32 = nullptr;
@@ -401,13 +447,14 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
     t32 = new ptg_tensor(*t);
     t32->dtype = PTG_F32;
     t32->owns = true;
+    t32->f8_scales = nullptr;
     int rs = PTG_OK;
     if (storage32) {
       rs = storage32->ensure((size_t)t->numel_padded * 4);
       t32->data = storage32->ptr;
       t32->owns = false;
-    } else if ((e = cudaMalloc(&t32->data, (size_t)t->numel_padded * 4)) != cudaSuccess) {
-      rs = cuda_error(e, "cudaMalloc(tensor)", __FILE__, __LINE__);
+    } else {
+      rs = ctx_malloc(c, &t32->data, (size_t)t->numel_padded * 4, "tensor");
     }
     if (rs != PTG_OK) {
       if (t->owns) cudaFree(t->data);
@@ -421,8 +468,11 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
   const int64_t nfib = numel / I0;
   // staging for host sources: two chunk buffers, copies on `side`, conversion on `stream`
   // (a device source is converted in one launch; a host source streams through 64 MB chunks)
-  const int64_t chunk_fib =
+  // (FP8: a chunk holds whole slabs, whose maxima set the scales before they are encoded)
+  const int64_t fps = nfib / nslab;   // mode-0 fibres per slab
+  int64_t chunk_fib =
       src_on_device ? nfib : std::max<int64_t>(1, std::min<int64_t>(nfib, (64ll << 20) / I0));
+  if (fp8 && !src_on_device) chunk_fib = std::min<int64_t>(nfib, std::max<int64_t>(1, chunk_fib / fps) * fps);
   double *stage[2] = {nullptr, nullptr};
   double *part = nullptr, *acc = nullptr;
   cudaEvent_t copied[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
@@ -441,6 +491,7 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
       break;
     }
     cudaMemsetAsync(acc, 0, sizeof(double) * 2, c->stream);
+    if (fp8) cudaMemsetAsync(slab_bits, 0, sizeof(unsigned long long) * nslab, c->stream);
     if (!src_on_device) {
       for (int b = 0; b < 2 && rc == PTG_OK; ++b) {
         if ((e = cudaMalloc(&stage[b], sizeof(double) * chunk_fib * I0)) != cudaSuccess)
@@ -471,7 +522,17 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
         csrc = stage[b];
       }
       const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(kConvBlocks, nf));
-      if (dtype == PTG_F32)
+      if (fp8) {
+        int r8 = f8_slab_max_launch(csrc, I0, f0, nf, fps, slab_bits, c->sm_count, c->stream);
+        if (r8 == PTG_OK)
+          r8 = f8_encode_launch(csrc, I0, pI0, f0, nf, fps, slab_bits, (uint8_t *)t->data, d32, t->f8_scales, part,
+                                blocks, c->stream);
+        if (r8 != PTG_OK) {
+          fail(r8);
+          break;
+        }
+        count_launches(c, 1);
+      } else if (dtype == PTG_F32)
         convert_kernel<float><<<blocks, kConvThreads, 0, c->stream>>>(
             csrc, I0, pI0, f0, nf, (float *)t->data, nullptr, part);
       else
@@ -496,6 +557,15 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
     t->frob64 = h[0];
     t->frob_stored = h[1];
     if (t32) t32->frob64 = t32->frob_stored = h[0];   // the FP32 copy stores exactly the squared values summed
+    if (fp8) {   // the largest slab scale bounds the scaled Khatri-Rao values of the MTTKRP
+      std::vector<float> sc((size_t)nslab);
+      e = cudaMemcpy(sc.data(), t->f8_scales, sizeof(float) * nslab, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) {
+        fail(cuda_error(e, "cudaMemcpy(slab scales)", __FILE__, __LINE__));
+        break;
+      }
+      t->f8_scale_max = *std::max_element(sc.begin(), sc.end());
+    }
     if (!std::isfinite(h[0]) || !std::isfinite(h[1]))
       fail(set_error(PTG_ERR_NUMERIC, "tensor contains NaN or Inf"));
   } while (0);
@@ -537,6 +607,14 @@ int ptg_tensor_norms(const ptg_tensor *t, double *frob64, double *frob_stored) {
   if (!t) return set_error(PTG_ERR_INVALID, "tensor is NULL");
   if (frob64) *frob64 = t->frob64;
   if (frob_stored) *frob_stored = t->frob_stored;
+  return PTG_OK;
+}
+
+int ptg_tensor_storage(const ptg_tensor *t, const void **data, int64_t *padded_dim0, const float **slab_scales) {
+  if (!t) return set_error(PTG_ERR_INVALID, "tensor is NULL");
+  if (data) *data = t->data;
+  if (padded_dim0) *padded_dim0 = t->pdim0;
+  if (slab_scales) *slab_scales = t->f8_scales;
   return PTG_OK;
 }
 

@@ -90,6 +90,10 @@ Contraction node_contraction(const ptg_tensor *t, const float *const *factors, b
     for (int k = h; k < N; ++k) c.Q *= ext(k);
   }
   c.q_write = c.Q;
+  // the last mode's index: the slowest digit of s (left node) or of q (right node)
+  c.slab_div = 1;
+  for (int k = h; k < N - 1; ++k) c.slab_div *= ext(k);
+  c.slab_in_q = !left_node;
   return c;
 }
 

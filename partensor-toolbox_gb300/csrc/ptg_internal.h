@@ -35,6 +35,7 @@ int cuda_error(cudaError_t e, const char *what, const char *file, int line);
 struct DevBuf {
   void *ptr = nullptr;
   size_t bytes = 0;
+  const long long *limit = nullptr;   // the owning context's allocation limit (0: none)
   int ensure(size_t need);
   void release();
 };
@@ -73,6 +74,9 @@ struct ptg_ctx {
   int mttkrp_impl = 0;                // PTG_OPT_MTTKRP_IMPL
   int gtc_rows = 0;                   // PTG_OPT_GTC_ROWS
   int *dev_err = nullptr;             // device error word written by bounded waits
+  long long spin_limit = -1;          // PTG_OPT_SPIN_LIMIT (-1: the kernels' default)
+  long long alloc_limit = 0;          // PTG_OPT_ALLOC_LIMIT (0: none)
+  void *f8_work = nullptr;            // FP8 MTTKRP: column-maxima work words + column scales
   std::map<std::string, int> tuned;   // autotuner choices (batched CPD split-K target)
   // buffers of the one-call entry points (ptg_cpd, ptg_cpd_dimtree), kept between calls:
   // the stored tensor and its FP32 copy
@@ -96,6 +100,10 @@ struct ptg_tensor {
   double frob_stored = 0.0; // ||X||^2 of the stored copy
   bool owns = true;         // false: data lives in a context-owned buffer
   int device = 0;
+  // FP8 storage: the scale of each index of the last mode (inside the data allocation) and
+  // the largest of them
+  float *f8_scales = nullptr;
+  float f8_scale_max = 1.0f;
 };
 
 namespace ptg {
@@ -133,6 +141,10 @@ struct Contraction {
   KrSide before, after;
   int64_t q_write = 0;  // rows of `out` written (q < q_write)
   const int *skip = nullptr;   // device word: when nonzero at launch time the kernels do nothing
+  // where the index of the tensor's last mode (the FP8 slab) sits: slab = s / slab_div, or
+  // q / slab_div when slab_in_q (0: not set)
+  int64_t slab_div = 0;
+  bool slab_in_q = false;
 };
 
 // Build the contraction of a mode-n MTTKRP of tensor t.
@@ -168,6 +180,27 @@ int launch_leaf_mttkrp(ptg_ctx *ctx, const ptg_tensor *t, const float *T, const 
 // tcgen05 (tensor-core) form of contraction_launch; BF16 storage only.
 int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                           cudaStream_t stream);
+// FP8 (e4m3, per-slab scales) storage on the tensor cores (tcgen05 kind::f8f6f4), R <= 128.
+int f8_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
+                          cudaStream_t stream);
+// FP8 upload (ptg_fp8.cu): the max |x| of the slabs met by a run of mode-0 fibres, then the
+// codes, the slab scales, an optional FP32 copy and the FP64 partial sums of squares.
+int f8_slab_max_launch(const double *src, int64_t I0, int64_t fiber0, int64_t nfib, int64_t fps,
+                       unsigned long long *slab_bits, int sm_count, cudaStream_t s);
+int f8_encode_launch(const double *src, int64_t I0, int64_t pI0, int64_t fiber0, int64_t nfib, int64_t fps,
+                     const unsigned long long *slab_bits, uint8_t *dst, float *dst32, float *scales, double *part,
+                     int blocks, cudaStream_t s);
+// poll limit of the tensor-core kernels' bounded waits under this context
+constexpr uint32_t kDefaultSpinLimit = 1u << 26;
+uint32_t spin_limit(const ptg_ctx *ctx);
+// cudaMalloc under the context's allocation limit (PTG_OPT_ALLOC_LIMIT)
+int ctx_malloc(const ptg_ctx *ctx, void **p, size_t bytes, const char *what);
+// ||X||^2 in the ALS cost f^2 = ||X||^2 - 2 <M, A> + 1^T (Z .* G) 1: that of the stored copy,
+// except on FP8 storage, whose dithered copy is unbiased but carries the rounding noise's
+// energy in its own norm: there the FP64 source norm makes f^2 estimate the data's cost
+inline double cost_norm(const ptg_tensor *t) {
+  return t->dtype == PTG_FP8E4M3 ? t->frob64 : t->frob_stored;
+}
 // FP32 storage on the tensor cores (tcgen05 kind::tf32, three-term split), R <= 64.
 int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
                             cudaStream_t stream);

@@ -717,6 +717,11 @@ Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors,
     c.after.n++;
   }
   c.q_write = t->dims[mode];
+  // the last mode's index: the slowest digit of s, or q itself for the last mode
+  c.slab_div = 1;
+  c.slab_in_q = (mode == N - 1);
+  if (!c.slab_in_q)
+    for (int k = mode + 1; k < N - 1; ++k) c.slab_div *= ext(k);
   return c;
 }
 
@@ -725,8 +730,8 @@ Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors,
 static double contraction_bytes(const ptg_tensor *t, const Contraction &c, int R) {
   double numel = 1.0;
   for (int k = 0; k < t->order; ++k) numel *= (double)t->dims[k];
-  const double esz = t->dtype == PTG_F32 ? 4.0 : 2.0;
-  double fac = 0.0;
+  const double esz = t->dtype == PTG_F32 ? 4.0 : t->dtype == PTG_BF16 ? 2.0 : 1.0;
+  double fac = t->dtype == PTG_FP8E4M3 ? (double)t->dims[t->order - 1] * 4.0 : 0.0;   // slab scales
   for (int i = 0; i < c.before.n; ++i) fac += (double)c.before.valid[i] * R * 4.0;
   for (int i = 0; i < c.after.n; ++i) fac += (double)c.after.valid[i] * R * 4.0;
   return numel * esz + fac + (double)c.q_write * R * 4.0;
@@ -735,7 +740,7 @@ static double contraction_bytes(const ptg_tensor *t, const Contraction &c, int R
 // FP32 storage reaches the tensor cores (three-term TF32 split) only on request: its
 // accumulation in TMEM carries a small negative bias that grows with the contraction length
 bool contraction_uses_tc(const ptg_ctx *ctx, const ptg_tensor *t, int R) {
-  return (t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 128) ||
+  return t->dtype == PTG_FP8E4M3 || (t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 128) ||
          (t->dtype == PTG_F32 && R <= 64 && ctx->mttkrp_impl == 2);
 }
 
@@ -753,7 +758,9 @@ int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, 
   if (timed) PTG_TRY(stats_begin(ctx, stream, &ev));
   int rc;
   const bool tc = contraction_uses_tc(ctx, t, R);
-  if (t->dtype == PTG_F32 && tc)
+  if (t->dtype == PTG_FP8E4M3)
+    rc = f8_contraction_launch(ctx, t, c, R, out, stream);
+  else if (t->dtype == PTG_F32 && tc)
     rc = tc32_contraction_launch(ctx, t, c, R, out, stream);
   else if (t->dtype == PTG_F32)
     rc = launch_typed<float>(ctx, t, c, R, out, stream);

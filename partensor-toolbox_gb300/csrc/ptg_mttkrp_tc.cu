@@ -40,6 +40,7 @@ struct TcParams {
   int R;
   int mmajor;
   uint32_t tmem_cols;
+  uint32_t spin;   // poll limit of every bounded wait
   KrDevTc before, after;
   float *partial;  // [nsplit][Q][N]
   int *err;
@@ -104,13 +105,14 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
     if (lane == 0 && nkb > 0) {
       int stage = 0;
       uint32_t phase = 0;
-      for (int kb = 0; kb < nkb; ++kb) {
+      int issued[TC_STAGES] = {0};   // loads issued into each stage
+      bool ok = true;
+      for (int kb = 0; kb < nkb && ok; ++kb) {
         const int64_t t = kb0 + kb;
         for (int m = 0; m < nqt; ++m) {
-          if (!mbar_wait(&empty_a[stage], phase ^ 1, abort_flag)) {
-            *abort_flag = 1;
-            atomicExch(prm.err, PTG_ERR_TIMEOUT);
-            goto producer_done;
+          if (!mbar_wait_lim(&empty_a[stage], phase ^ 1, abort_flag, prm.spin)) {
+            ok = false;
+            break;
           }
           mbar_expect_tx(&full_a[stage], TC_ATILE);
           uint8_t *dst = aring + stage * TC_ATILE;
@@ -124,13 +126,22 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
             const int p0 = (int)((t % prm.pblocks) * TC_BK);
             tma_load_3d(dst, &tmap, &full_a[stage], p0, q, s);
           }
+          ++issued[stage];
           if (++stage == TC_STAGES) {
             stage = 0;
             phase ^= 1;
           }
         }
       }
-    producer_done:;
+      if (!ok) {
+        *abort_flag = 1;
+        atomicExch(prm.err, PTG_ERR_TIMEOUT);
+      }
+      // a stage holds at most one load in flight (the next one waits for its release), the
+      // last one issued into it: wait for each so no copy lands after the CTA has exited
+      // (loads that were consumed completed long ago and return at once)
+      for (int s = 0; s < TC_STAGES; ++s)
+        if (issued[s] > 0) mbar_wait_bounded(&full_a[s], (uint32_t)((issued[s] - 1) & 1));
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
@@ -139,14 +150,14 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
       uint32_t phase = 0, kphase = 0;
       bool ok = true;
       for (int kb = 0; kb < nkb && ok; ++kb) {
-        if (!mbar_wait(&full_k[kst], kphase, abort_flag)) {
+        if (!mbar_wait_lim(&full_k[kst], kphase, abort_flag, prm.spin)) {
           ok = false;
           break;
         }
         tc_fence_after();
         const uint32_t kaddr = smem_u32(kring + kst * KTILE);
         for (int m = 0; m < nqt; ++m) {
-          if (!mbar_wait(&full_a[stage], phase, abort_flag)) {
+          if (!mbar_wait_lim(&full_a[stage], phase, abort_flag, prm.spin)) {
             ok = false;
             break;
           }
@@ -177,6 +188,8 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
         atomicExch(prm.err, PTG_ERR_TIMEOUT);
       }
       umma_commit(done);   // arrives once every MMA issued above has completed
+      // TMEM is released after the final barrier: the MMAs must have finished by then
+      mbar_wait_bounded(done, 0);
     }
   } else {
     // ---------------- Khatri-Rao builders (128 threads) ----------------
@@ -186,7 +199,7 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
     int kst = 0;
     uint32_t kphase = 0;
     for (int kb = 0; kb < nkb; ++kb) {
-      if (!mbar_wait(&empty_k[kst], kphase ^ 1, abort_flag)) {
+      if (!mbar_wait_lim(&empty_k[kst], kphase ^ 1, abort_flag, prm.spin)) {
         *abort_flag = 1;
         atomicExch(prm.err, PTG_ERR_TIMEOUT);
         break;
@@ -236,7 +249,7 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
       }
     }
     // ---------------- epilogue: TMEM -> partials ----------------
-    const bool have = (nkb > 0) && mbar_wait(done, 0, abort_flag) && !*abort_flag;
+    const bool have = (nkb > 0) && mbar_wait_lim(done, 0, abort_flag, prm.spin) && !*abort_flag;
     tc_fence_after();
     const int quarter = warp & 3;
     const int row = quarter * 32 + lane;
@@ -304,6 +317,7 @@ int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &
   prm.N = (R + 15) / 16 * 16;
   prm.R = R;
   prm.mmajor = mmajor ? 1 : 0;
+  prm.spin = spin_limit(ctx);
   auto cp = [](const KrSide &s) {
     KrDevTc d{};
     d.n = s.n;

@@ -229,7 +229,20 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
     const double margin = 16.0 * 1.1920929e-7 * s_scalar[1] + 1e-300;
     lo -= margin;
     hi += margin;
-    for (int round = 0; round < 8; ++round) {
+    // ... which holds while FP32 represents T well.  Where it does not (entries or their
+    // squares out of FP32 range, or counts off by more than the margin) the FP64 counts at
+    // the widened ends show it: then the FP64 multisection starts over from the Gershgorin
+    // interval, with enough rounds (33^16) to reach FP64 resolution from there.
+    int c_end = 0;
+    if (j < 2) c_end = sturm_count_f64(d, e2, n, j == 0 ? lo : hi);
+    const int c_lo = __shfl_sync(0xffffffffu, c_end, 0), c_hi = __shfl_sync(0xffffffffu, c_end, 1);
+    int rounds64 = 8;
+    if (!(c_lo < target && c_hi >= target)) {
+      lo = lohi[which][0];
+      hi = lohi[which][1];
+      rounds64 = 16;
+    }
+    for (int round = 0; round < rounds64; ++round) {
       const double x = lo + (hi - lo) * (double)(j + 1) / 33.0;
       const bool hit = sturm_count_f64(d, e2, n, x) >= target;
       const unsigned m = __ballot_sync(0xffffffffu, hit);

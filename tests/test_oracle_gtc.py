@@ -141,3 +141,23 @@ def test_local_l_nesterov_reaches_row_kkt():
         scale = max(1.0, np.abs(M[i]).max())
         assert grad.min() > -1e-6 * scale                       # dual feasibility
         assert np.abs(grad * A[i]).max() < 1e-6 * scale ** 2    # complementarity
+
+
+@pytest.mark.parametrize("stochastic", [False, True])
+def test_c_restatement_matches_numpy_oracle(stochastic):
+    """oracle/gtc_omp.c (the CPU baseline of the sparse workload) against oracle/gtc.py, one
+    factor update of every mode: local_L (NesterovMNLS.hpp:878-976) or the stochastic block
+    solver (:553-663)."""
+    from oracle import gtc as og
+    from oracle import omp
+    dims, R = [30, 25, 20], 5
+    idx, vals, _ = og.make_gtc_problem(dims, 3000, R, seed=1)
+    init = [np.random.default_rng(k).random((I, R)) for k, I in enumerate(dims)]
+    for n in range(3):
+        mm = og.matricize(idx, vals, dims, n)
+        if stochastic:
+            ref = og.stochastic_nesterov(init, mm, 0.3, 20, 1e-3, 7, 3)
+        else:
+            ref = og.local_L_nesterov(init, mm, og.sparse_mttkrp(init, mm), 20, 1e-3)
+        got = omp.gtc_rows(mm.ptr, mm.other, mm.vals, init, n, stochastic, 0.3, 20, 1e-3, seed=7, outer=3)
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
