@@ -159,7 +159,9 @@ int ptg_mttkrp(ptg_ctx *ctx, const ptg_tensor *X, const float *const *factors, i
  * 32, 64 or 128); larger calls return PTG_ERR_UNSUPPORTED.  The first call on a device looks
  * up the block's address on that device: make it before any stream capture.  Calls share the
  * block, so two calls that overlap on the GPU race; the block keeps the last call's data and
- * nothing in it needs clearing. */
+ * nothing in it needs clearing.  X, out, the factors and the stream must belong to the
+ * current device (X and out are checked: PTG_ERR_INVALID); the looked-up address is kept
+ * for the process, so the entry point must not be used across a cudaDeviceReset. */
 int ptg_mttkrp_noalloc(const float *X, int order, const int64_t *dims, int64_t ld0,
                        const float *const *factors, int rank, int mode, float *out, void *stream);
 

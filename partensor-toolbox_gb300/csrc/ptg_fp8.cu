@@ -219,7 +219,8 @@ constexpr int F8_BM = 128;          // q rows per tile (MMA M)
 constexpr int F8_BK = 128;          // contraction elements per K-block (one 128-byte row)
 constexpr int F8_MAX_STAGES = 8;    // X tile ring
 constexpr int F8_MAX_KSTAGES = 4;   // Khatri-Rao tile ring
-constexpr int F8_THREADS = 192;
+constexpr int F8_THREADS = 320;     // producer, MMA issuer, 8 Khatri-Rao builder warps
+constexpr int F8_BUILDERS = 256;
 constexpr int F8_ATILE = F8_BM * F8_BK;   // 16 KB
 constexpr int F8_WORK_WORDS = 2 * PTG_MAX_ORDER * 128 + 32;   // column maxima + ticket
 
@@ -234,6 +235,7 @@ struct F8Params {
   int stages, kstages;
   uint32_t tmem_cols;
   uint32_t spin;             // poll limit of every bounded wait
+  int vec4;                  // factor rows are read as float4 (R % 4 == 0, 16-byte aligned)
   KrDevTc before, after;
   const float *slab_scale;   // scale of each index of the last mode
   int64_t slab_div;          // slab = lin / slab_div, lin = s (slab_in_q == 0) or q
@@ -327,7 +329,7 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
       mbar_init(&empty_a[i], 1);
     }
     for (int i = 0; i < KSTAGES; ++i) {
-      mbar_init(&full_k[i], 128);
+      mbar_init(&full_k[i], F8_BUILDERS);
       mbar_init(&empty_k[i], 1);
     }
     mbar_init(done, 1);
@@ -446,8 +448,10 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
       mbar_wait_bounded(done, 0);
     }
   } else {
-    // ---------------- Khatri-Rao builders (128 threads, one K row each) ----------------
-    const int k = threadIdx.x - 64;
+    // ---------------- Khatri-Rao builders (256 threads: each K row by two threads) ----------------
+    const int k = (threadIdx.x - 64) & (F8_BK - 1);
+    const int part = (threadIdx.x - 64) >> 7;   // 16-column chunks part, part + 2, ...
+    const bool drains = warp < 6;               // warps 2..5 cover the four TMEM lane quarters
     int kst = 0;
     uint32_t kphase = 0;
     for (int kb = 0; kb < nkb; ++kb) {
@@ -472,21 +476,16 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
         lin_b = (uint32_t)p;
       }
       const float row_sc = (valid && !prm.slab_in_q) ? __ldg(prm.slab_scale + (int64_t)lin_a / prm.slab_div) : 1.0f;
-      for (int c = 0; c < RP; c += 8) {
-        float v[8], vb[8];
+      for (int c = 16 * part; c < RP; c += 32) {
+        float v[16];
         if (valid) {
-          kr8(prm.after, lin_a, prm.R, c, v);
-          if (!prm.mmajor) {
-            kr8(prm.before, lin_b, prm.R, c, vb);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) v[j] *= vb[j];
-          }
+          kr_pair<16>(prm.after, lin_a, prm.before, lin_b, !prm.mmajor, prm.R, c, prm.vec4 != 0, v);
         } else {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) v[j] = 0.0f;
+          for (int j = 0; j < 16; ++j) v[j] = 0.0f;
         }
 #pragma unroll
-        for (int j = 0; j < 8; j += 2) {
+        for (int j = 0; j < 16; j += 2) {
           const float a0 = v[j] * row_sc * cs[c + j], a1 = v[j + 1] * row_sc * cs[c + j + 1];
           const uint32_t hi = e4m3x2_rn(a0, a1);
           const float2 hb = e4m3x2_to_f32(hi);
@@ -506,11 +505,11 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
       }
     }
     // ---------------- epilogue: TMEM -> partials ----------------
-    const bool have = (nkb > 0) && mbar_wait_lim(done, 0, abort_flag, spin) && !*abort_flag;
+    const bool have = drains && (nkb > 0) && mbar_wait_lim(done, 0, abort_flag, spin) && !*abort_flag;
     tc_fence_after();
     const int quarter = warp & 3;
     const int row = quarter * 32 + lane;
-    for (int m = 0; m < nqt; ++m) {
+    for (int m = 0; drains && m < nqt; ++m) {
       const int64_t q = (int64_t)(qt0 + m) * F8_BM + row;
       float *dst = prm.partial + ((int64_t)split * prm.Q + q) * RP;
       const float qsc = (prm.slab_in_q && q < prm.Q) ? __ldg(prm.slab_scale + q / prm.slab_div) : 1.0f;
@@ -605,6 +604,7 @@ int f8_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &
   };
   prm.before = cp(c.before);
   prm.after = cp(c.after);
+  prm.vec4 = kr_vec4_ok(c, R) ? 1 : 0;
   prm.slab_scale = t->f8_scales;
   prm.slab_div = c.slab_div;
   prm.slab_in_q = c.slab_in_q ? 1 : 0;

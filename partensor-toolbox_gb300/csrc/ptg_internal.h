@@ -147,6 +147,17 @@ struct Contraction {
   bool slab_in_q = false;
 };
 
+// Whether the factor rows of a contraction can be read as float4: R % 4 == 0 and every
+// factor 16-byte aligned.
+inline bool kr_vec4_ok(const Contraction &c, int R) {
+  if (R % 4 != 0) return false;
+  for (int i = 0; i < c.before.n; ++i)
+    if (reinterpret_cast<uintptr_t>(c.before.fac[i]) % 16 != 0) return false;
+  for (int i = 0; i < c.after.n; ++i)
+    if (reinterpret_cast<uintptr_t>(c.after.fac[i]) % 16 != 0) return false;
+  return true;
+}
+
 // Build the contraction of a mode-n MTTKRP of tensor t.
 Contraction mttkrp_contraction(const ptg_tensor *t, const float *const *factors, int mode);
 

@@ -41,6 +41,7 @@ struct TcParams {
   int mmajor;
   uint32_t tmem_cols;
   uint32_t spin;   // poll limit of every bounded wait
+  int vec4;        // factor rows are read as float4 (R % 4 == 0, 16-byte aligned)
   KrDevTc before, after;
   float *partial;  // [nsplit][Q][N]
   int *err;
@@ -220,25 +221,36 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
         lin_a = (uint32_t)s;
         lin_b = (uint32_t)p;
       }
-      for (int c = nhalf * ncols; c < (nhalf + 1) * ncols; c += 8) {
-        float va[8], vb[8];
-        if (valid) {
-          kr8(prm.after, lin_a, prm.R, c, va);
-          if (!prm.mmajor) {
-            kr8(prm.before, lin_b, prm.R, c, vb);
+      // the thread's columns in chunks of 16 (8 when it has fewer), the loads of a chunk's
+      // factor rows issued together
+      auto put = [&](int n, float v) {
+        const uint32_t off = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128 + ((((k >> 3) ^ (n & 7)) & 7) << 4) +
+                                        (k & 7) * 2);
+        *reinterpret_cast<__nv_bfloat16 *>(kt + off) = __float2bfloat16_rn(v);
+      };
+      if (ncols % 16 == 0) {
+        for (int c = nhalf * ncols; c < (nhalf + 1) * ncols; c += 16) {
+          float va[16];
+          if (valid) {
+            kr_pair<16>(prm.after, lin_a, prm.before, lin_b, !prm.mmajor, prm.R, c, prm.vec4 != 0, va);
+          } else {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) va[j] *= vb[j];
+            for (int j = 0; j < 16; ++j) va[j] = 0.0f;
           }
-        } else {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) va[j] = 0.0f;
+          for (int j = 0; j < 16; ++j) put(c + j, va[j]);
         }
+      } else {
+        for (int c = nhalf * ncols; c < (nhalf + 1) * ncols; c += 8) {
+          float va[8];
+          if (valid) {
+            kr_pair<8>(prm.after, lin_a, prm.before, lin_b, !prm.mmajor, prm.R, c, prm.vec4 != 0, va);
+          } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const int n = c + j;
-          const uint32_t off = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128 + ((((k >> 3) ^ (n & 7)) & 7) << 4) +
-                                          (k & 7) * 2);
-          *reinterpret_cast<__nv_bfloat16 *>(kt + off) = __float2bfloat16_rn(va[j]);
+            for (int j = 0; j < 8; ++j) va[j] = 0.0f;
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j) put(c + j, va[j]);
         }
       }
       fence_async_smem();
@@ -330,6 +342,7 @@ int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &
   };
   prm.before = cp(c.before);
   prm.after = cp(c.after);
+  prm.vec4 = kr_vec4_ok(c, R) ? 1 : 0;
   prm.qtiles = (int)((c.Q + TC_BM - 1) / TC_BM);
   int mt = std::max(1, 512 / prm.N);
   mt = std::min(mt, prm.qtiles);

@@ -18,6 +18,11 @@
 // needs to start at zero: each call writes every partial it later reads.  Two calls whose
 // kernels overlap on the GPU (different streams, or the same stream from different host
 // threads without ordering) race on the block.
+//
+// The looked-up address is kept for the life of the process.  A cudaDeviceReset (or any
+// teardown of the device's primary context) reloads the module at a new address, so the
+// entry point must not be used across one.  X, out, the factors and the stream must belong
+// to the current device; X and out are checked.
 #include <mutex>
 
 #include "ptg_internal.h"
@@ -68,6 +73,14 @@ extern "C" int ptg_mttkrp_noalloc(const float *X, int order, const int64_t *dims
   if ((reinterpret_cast<uintptr_t>(X) & 15) != 0) return set_error(PTG_ERR_INVALID, "X must be 16-byte aligned");
   int device = 0;
   PTG_CUDA(cudaGetDevice(&device));
+  // the buffers must live on the current device, whose copy of the block the kernel uses
+  for (const void *p : {static_cast<const void *>(X), static_cast<const void *>(out)}) {
+    cudaPointerAttributes a;
+    PTG_CUDA(cudaPointerGetAttributes(&a, p));
+    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged)
+      return set_error(PTG_ERR_INVALID, "X and out must be device memory");
+    if (a.device != device) return set_error(PTG_ERR_INVALID, "X and out must belong to the current device");
+  }
   int sms = 0;
   PTG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   // a stack description of the caller's tensor (no allocation)

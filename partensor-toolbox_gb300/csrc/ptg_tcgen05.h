@@ -204,6 +204,93 @@ __device__ __forceinline__ void kr4(const KrDevTc &s, uint32_t lin, int R, int c
   }
 }
 
+// The rows of the first two factors of one side for the digits of `lin` (null when the side
+// has fewer factors), and whether every digit lies within its factor's valid rows (a padded
+// mode-0 index makes the Khatri-Rao value zero; its row address then points at row 0, so no
+// load leaves the factor).  Kept in registers: no per-thread arrays.
+struct KrRows2 {
+  const float *r0, *r1;
+  bool ok;
+};
+__device__ __forceinline__ KrRows2 kr_rows2(const KrDevTc &s, uint32_t lin, int R) {
+  KrRows2 o{nullptr, nullptr, true};
+  for (int f = 0; f < s.n; ++f) {
+    const uint32_t e = s.ext[f];
+    const uint32_t d = lin % e;
+    lin /= e;
+    const bool in = d < s.valid[f];
+    o.ok = o.ok && in;
+    const float *p = s.fac[f] + (size_t)(in ? d : 0u) * R;
+    if (f == 0) o.r0 = p;
+    else if (f == 1) o.r1 = p;
+  }
+  return o;
+}
+
+// W consecutive values of a factor row from column c (0 beyond R; 1 when row is null, the
+// neutral factor of an empty side).  vec: R % 4 == 0 and 16-byte aligned rows, so float4.
+template <int W>
+__device__ __forceinline__ void kr_load(const float *row, int R, int c, bool vec, float *t) {
+  if (vec) {
+#pragma unroll
+    for (int q = 0; q < W / 4; ++q) {
+      float4 x = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+      if (row) x = (c + 4 * q < R) ? __ldg(reinterpret_cast<const float4 *>(row + c + 4 * q))
+                                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      t[4 * q] = x.x;
+      t[4 * q + 1] = x.y;
+      t[4 * q + 2] = x.z;
+      t[4 * q + 3] = x.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < W; ++j) t[j] = row ? ((c + j < R) ? __ldg(row + c + j) : 0.0f) : 1.0f;
+  }
+}
+
+// Factors 2, 3, ... of one side multiplied into v (a side has more than two factors only
+// for orders >= 4 on the before side or >= 5 on the after side).
+template <int W>
+__device__ __forceinline__ void kr_tail(const KrDevTc &s, uint32_t lin, int R, int c, bool vec, float *v) {
+  for (int f = 0; f < s.n; ++f) {
+    const uint32_t e = s.ext[f];
+    const uint32_t d = lin % e;
+    lin /= e;
+    if (f < 2) continue;
+    float t[W];
+    kr_load<W>(s.fac[f] + (size_t)(d < s.valid[f] ? d : 0u) * R, R, c, vec, t);
+#pragma unroll
+    for (int j = 0; j < W; ++j) v[j] *= t[j];
+  }
+}
+
+// Khatri-Rao values of columns [c, c + W) for the K row (lin_a on the "after" side, lin_b on
+// the "before" side when use_b): (1 * a_0 * a_1 ...) * (1 * b_0 * b_1 ...), the order of kr8.
+// The first two factors of each side are loaded before any product is formed, so a 3- or
+// 4-way contraction pays one memory round trip per call.
+template <int W>
+__device__ __forceinline__ void kr_pair(const KrDevTc &A, uint32_t lin_a, const KrDevTc &B, uint32_t lin_b,
+                                        bool use_b, int R, int c, bool vec, float *v) {
+  const KrRows2 ra = kr_rows2(A, lin_a, R);
+  KrRows2 rb{nullptr, nullptr, true};
+  if (use_b) rb = kr_rows2(B, lin_b, R);
+  float a0[W], a1[W], b0[W], b1[W];
+  kr_load<W>(ra.r0, R, c, vec, a0);
+  kr_load<W>(ra.r1, R, c, vec, a1);
+  kr_load<W>(rb.r0, R, c, vec, b0);
+  kr_load<W>(rb.r1, R, c, vec, b1);
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    a0[j] = ra.r1 ? a0[j] * a1[j] : a0[j];
+    b0[j] = rb.r1 ? b0[j] * b1[j] : b0[j];
+  }
+  if (A.n > 2) kr_tail<W>(A, lin_a, R, c, vec, a0);
+  if (use_b && B.n > 2) kr_tail<W>(B, lin_b, R, c, vec, b0);
+  const bool ok = ra.ok && rb.ok;
+#pragma unroll
+  for (int j = 0; j < W; ++j) v[j] = ok ? (use_b ? a0[j] * b0[j] : a0[j]) : 0.0f;
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,

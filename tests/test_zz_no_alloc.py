@@ -74,3 +74,40 @@ def test_noalloc_rejects_sizes_beyond_the_block(pkg):
     # a misaligned stride is refused too
     rc = _noalloc(lib, X, [7, 8, 8], 7, facs, R, 1, out)
     assert rc == pkg._lib.PTG_ERR_INVALID
+    # mode 0 is limited by the padded stride: 65536 x 32 columns fits, 65544 x 32 does not
+    X2 = torch.zeros(65544 * 64, device="cuda")
+    facs2 = [torch.zeros(I, R, device="cuda") for I in (65536, 8, 8)]
+    out2 = torch.zeros(65536, R, device="cuda")
+    assert _noalloc(lib, X2, [65536, 8, 8], 65536, facs2, R, 0, out2) == 0, lib.ptg_last_error().decode()
+    torch.cuda.synchronize()
+    rc = _noalloc(lib, X2, [65536, 8, 8], 65544, facs2, R, 0, out2)
+    assert rc == pkg._lib.PTG_ERR_UNSUPPORTED
+    # host memory is refused
+    host = torch.zeros(ld0 * 64)
+    assert _noalloc(lib, host, dims, ld0, facs, R, 1, out) == pkg._lib.PTG_ERR_INVALID
+
+
+def test_noalloc_allocates_nothing(pkg):
+    """After a first call (which looks up the block's address), calls of several shapes leave
+    the device's free memory and torch's allocated bytes unchanged."""
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    lib = pkg._lib.load()
+    rng = np.random.default_rng(5)
+    cases = []
+    for dims, R in [((37, 29, 23), 7), ((64, 48, 40), 32), ((20, 12, 10, 8), 40), ((128, 16, 9), 100)]:
+        X = rng.random(dims)
+        ld0 = (dims[0] + 7) // 8 * 8
+        facs = [torch.tensor(rng.random((I, R)), dtype=torch.float32, device="cuda") for I in dims]
+        outs = [torch.empty(dims[m], R, device="cuda") for m in range(len(dims))]
+        cases.append((_padded(X, ld0), list(dims), ld0, facs, R, outs))
+    Xd, dims, ld0, facs, R, outs = cases[0]
+    assert _noalloc(lib, Xd, dims, ld0, facs, R, 0, outs[0]) == 0
+    torch.cuda.synchronize()
+    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    for Xd, dims, ld0, facs, R, outs in cases:
+        for m in range(len(dims)):
+            assert _noalloc(lib, Xd, dims, ld0, facs, R, m, outs[m]) == 0, lib.ptg_last_error().decode()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_allocated() == alloc0
