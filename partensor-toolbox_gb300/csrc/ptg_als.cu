@@ -29,7 +29,8 @@ struct AlsBuffers {
   float *gram[PTG_MAX_ORDER] = {nullptr};
   float *gacc[PTG_MAX_ORDER] = {nullptr};
   float *M = nullptr;
-  float *TL = nullptr, *TR = nullptr;   // dimension-tree node tensors (when used)
+  float *TL = nullptr, *TR = nullptr;   // dimension-tree node tensors of the root's children
+  float *TD = nullptr;                  // the deeper node tensors (orders >= 5)
   float *gpart = nullptr;
   NnlsParams *np = nullptr;
   double *dsc = nullptr;  // [N][2]: <M, A>, sum(Z .* G); [0][2..3]: cost terms of a point;
@@ -41,7 +42,7 @@ struct AlsBuffers {
   void *base = nullptr;
 
   int alloc(const ptg_ctx *ctx, const int64_t *dims, int order, int rank, int64_t rows_left = 0,
-            int64_t rows_right = 0) {
+            int64_t rows_right = 0, size_t deep_floats = 0) {
     N = order;
     R = rank;
     size_t off = 0;
@@ -68,6 +69,7 @@ struct AlsBuffers {
     const size_t o_M = take(sizeof(float) * maxrows * R);
     const size_t o_TL = take(sizeof(float) * std::max<int64_t>(rows_left, 1) * R);
     const size_t o_TR = take(sizeof(float) * std::max<int64_t>(rows_right, 1) * R);
+    const size_t o_TD = take(sizeof(float) * std::max<size_t>(deep_floats, 1));
     const size_t o_gp = take(sizeof(float) * gp);
     const size_t o_np = take(sizeof(NnlsParams));
     const size_t o_d = take(sizeof(double) * (4 * N + 2));
@@ -91,6 +93,7 @@ struct AlsBuffers {
     M = (float *)(b + o_M);
     TL = (float *)(b + o_TL);
     TR = (float *)(b + o_TR);
+    TD = (float *)(b + o_TD);
     gpart = (float *)(b + o_gp);
     np = (NnlsParams *)(b + o_np);
     dsc = (double *)(b + o_d);
@@ -175,6 +178,7 @@ struct Runner {
   int weight = 0;
   bool all_orth = true;
   bool dimtree = false;
+  DimTree tree;                   // the dimension tree's nodes and their freshness (dimtree)
   WarmArgs warm[PTG_MAX_ORDER];   // per mode, for the sweep being run
   std::chrono::steady_clock::time_point t0;
 
@@ -192,6 +196,7 @@ struct Runner {
   int sweep_enqueue(const ptg_tensor *X) {
     cudaStream_t S = ctx->stream, T = ctx->side;
     const int N = b.N, R = b.R;
+    if (dimtree) tree.new_sweep();   // normalisation and the line search changed every factor
     for (int n = 0; n < N; ++n) {
       const int con = opt->constraints[n];
       if (con != PTG_NONNEGATIVITY) {
@@ -209,18 +214,16 @@ struct Runner {
         Contraction c = mttkrp_contraction(X, b.fac, n);
         PTG_TRY(contraction_launch(ctx, X, c, R, b.M, S));
       } else {
-        // node tensors: the left node before mode 0 (current right-half factors), the
-        // right node before the first right-half mode (updated left-half factors)
-        const int h = dimtree_split(N);
-        if (n == 0) PTG_TRY(contraction_launch(ctx, X, node_contraction(X, b.fac, true), R, b.TL, S));
-        if (n == h) PTG_TRY(contraction_launch(ctx, X, node_contraction(X, b.fac, false), R, b.TR, S));
-        PTG_TRY(launch_leaf_mttkrp(ctx, X, n < h ? b.TL : b.TR, b.fac, n, R, b.M, S));
+        // through the tree: the nodes on the path to leaf n that a changed factor made stale
+        // are recomputed (the root's children once per sweep, before modes 0 and h)
+        PTG_TRY(tree.mttkrp(ctx, X, b.fac, n, R, b.M, S));
       }
       PTG_CUDA(cudaStreamWaitEvent(S, ctx->ev_join, 0));
       PTG_TRY(launch_nnls_full(ctx, b.M, b.fac[n], b.rows[n], R, b.np, (float)opt->nesterov_delta_1,
                                (float)opt->nesterov_delta_2, b.gram[n], b.dsc + 4 * n,
                                b.dsc + 4 * n + 1, b.isc + 2 * n, b.isc + 2 * n + 1, S, warm[n]));
       count_launches(ctx, 1);
+      if (dimtree) tree.updated(n);
     }
     HostScalars *h = hs();
     PTG_CUDA(cudaMemcpyAsync(h->dsc, b.dsc, sizeof(double) * 4 * N, cudaMemcpyDeviceToHost, S));
@@ -298,10 +301,7 @@ struct Runner {
       Contraction c = mttkrp_contraction(X, b.fac, n);
       return contraction_launch(ctx, X, c, b.R, b.M, S);
     }
-    const int h = dimtree_split(b.N);
-    if (n == 0) PTG_TRY(contraction_launch(ctx, X, node_contraction(X, b.fac, true), b.R, b.TL, S));
-    if (n == h) PTG_TRY(contraction_launch(ctx, X, node_contraction(X, b.fac, false), b.R, b.TR, S));
-    return launch_leaf_mttkrp(ctx, X, n < h ? b.TL : b.TR, b.fac, n, b.R, b.M, S);
+    return tree.mttkrp(ctx, X, b.fac, n, b.R, b.M, S);
   }
 
   // update_factor for the constraints other than nonnegativity (include/Cpd.hpp:196-222),
@@ -321,6 +321,7 @@ struct Runner {
       return set_error(PTG_ERR_INVALID, "unknown constraint");
     }
     PTG_TRY(launch_gram(b.fac[n], b.rows[n], R, b.gram[n], b.gpart, S));
+    if (dimtree) tree.updated(n);
     count_launches(ctx, 2);
     PTG_CUDA(cudaMemsetAsync(b.isc + 2 * n, 0, 2 * sizeof(int), S));
     if (n == N - 1) {
@@ -420,7 +421,10 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
   Runner run{ctx, &opt};
   run.t0 = std::chrono::steady_clock::now();
   run.dimtree = dimtree;
-  PTG_TRY(run.b.alloc(ctx, X->dims, N, rank, dimtree ? node_rows(X, true) : 0, dimtree ? node_rows(X, false) : 0));
+  if (dimtree) PTG_TRY(run.tree.build(X));
+  PTG_TRY(run.b.alloc(ctx, X->dims, N, rank, dimtree ? node_rows(X, true) : 0, dimtree ? node_rows(X, false) : 0,
+                      dimtree ? run.tree.deep_floats(rank) : 0));
+  if (dimtree) run.tree.bind(run.b.TL, run.b.TR, run.b.TD, rank);
   AlsBuffers &b = run.b;
   cudaStream_t S = ctx->stream;
 

@@ -181,12 +181,39 @@ const float *mlp_theta(const ptg_mlp *m);
 int mlp_din(const ptg_mlp *m);
 int mlp_hidden(const ptg_mlp *m);
 
-// Dimension tree (ptg_dimtree.cu): split point, node contraction, node size, leaf MTTKRP.
+// Dimension tree (ptg_dimtree.cu): split point, the root children's contractions and sizes,
+// and the tree of node tensors with its lazy updates.
 int dimtree_split(int order);
 Contraction node_contraction(const ptg_tensor *t, const float *const *factors, bool left_node);
 int64_t node_rows(const ptg_tensor *t, bool left_node);
-int launch_leaf_mttkrp(ptg_ctx *ctx, const ptg_tensor *t, const float *T, const float *const *factors, int mode,
-                       int R, float *out, cudaStream_t stream);
+class DimTree {
+ public:
+  struct Node {
+    int a, b;          // modes [a, b)
+    int parent;
+    int child[2];
+    int64_t rows;      // prod of the node's mode extents (mode 0 padded)
+    float *T;          // [rows][R], resident (null for leaves)
+    long long at;      // step at which it was computed (-1: never)
+  };
+  int build(const ptg_tensor *t);                  // the structure; deep_floats() after it
+  size_t deep_floats(int R) const { return deep * (size_t)R; }   // nodes below the root's children
+  void bind(float *left, float *right, float *deep_base, int R);
+  void new_sweep();                                // every factor changed since the last sweep
+  void updated(int mode);                          // factor `mode` changed
+  // M_n into out: the stale nodes on the path to the leaf recomputed first
+  int mttkrp(ptg_ctx *ctx, const ptg_tensor *X, const float *const *factors, int mode, int R, float *out,
+             cudaStream_t s);
+  const std::vector<Node> &all() const { return nodes; }
+
+ private:
+  bool fresh(const Node &nd) const;
+  std::vector<Node> nodes;
+  int N = 0;
+  size_t deep = 0;
+  long long last[PTG_MAX_ORDER] = {0};
+  long long step = 0;
+};
 
 // tcgen05 (tensor-core) form of contraction_launch; BF16 storage only.
 int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,

@@ -7,8 +7,10 @@
 //               (128-byte swizzle; K-major for modes n >= 1, MN-major for mode 0);
 //   warp 1      allocates TMEM and issues tcgen05.mma (M=128, N=R padded to 16, K=16) from
 //               one elected lane; each q-tile of the CTA accumulates in its own TMEM columns;
-//   warps 2..5  build the R x 64 Khatri-Rao tile of every K-block in shared memory (BF16,
-//               swizzled K-major), then drain TMEM (tcgen05.ld) into the split-K partials.
+//   warps 2..9  build the R x 64 Khatri-Rao tile of every K-block in shared memory (BF16,
+//               swizzled K-major; four threads per K row, one 8-column chunk each, the
+//               factor rows of a chunk loaded together); warps 2..5 then drain TMEM
+//               (tcgen05.ld) into the split-K partials.
 // Every mbarrier wait is bounded: on timeout the kernel raises an error word and returns
 // after releasing its TMEM.
 #include <cuda.h>
@@ -29,7 +31,8 @@ constexpr int TC_BM = 128;         // q rows per tile (MMA M)
 constexpr int TC_BK = 64;          // contraction elements per K-block (one 128-byte row)
 constexpr int TC_STAGES = 8;       // X tile ring
 constexpr int TC_KSTAGES = 4;      // Khatri-Rao tile ring
-constexpr int TC_THREADS = 192;
+constexpr int TC_THREADS = 320;    // producer, MMA issuer, 8 Khatri-Rao builder warps
+constexpr int TC_BUILDERS = 256;
 constexpr int TC_ATILE = TC_BM * TC_BK * 2;   // 16 KB
 
 struct TcParams {
@@ -79,7 +82,7 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
       mbar_init(&empty_a[i], 1);
     }
     for (int i = 0; i < TC_KSTAGES; ++i) {
-      mbar_init(&full_k[i], 128);
+      mbar_init(&full_k[i], TC_BUILDERS);
       mbar_init(&empty_k[i], 1);
     }
     mbar_init(done, 1);
@@ -193,10 +196,10 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
       mbar_wait_bounded(done, 0);
     }
   } else {
-    // ---------------- Khatri-Rao builders (128 threads) ----------------
+    // ---------------- Khatri-Rao builders (256 threads) ----------------
     const int tb = threadIdx.x - 64;
-    const int k = tb & 63, nhalf = tb >> 6;
-    const int ncols = N / 2;
+    const int k = tb & 63, part = tb >> 6;   // four threads per K row: 8-column chunks part, part + 4, ...
+    const bool drains = warp < 6;            // warps 2..5 cover the four TMEM lane quarters
     int kst = 0;
     uint32_t kphase = 0;
     for (int kb = 0; kb < nkb; ++kb) {
@@ -221,36 +224,21 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
         lin_a = (uint32_t)s;
         lin_b = (uint32_t)p;
       }
-      // the thread's columns in chunks of 16 (8 when it has fewer), the loads of a chunk's
-      // factor rows issued together
-      auto put = [&](int n, float v) {
-        const uint32_t off = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128 + ((((k >> 3) ^ (n & 7)) & 7) << 4) +
-                                        (k & 7) * 2);
-        *reinterpret_cast<__nv_bfloat16 *>(kt + off) = __float2bfloat16_rn(v);
-      };
-      if (ncols % 16 == 0) {
-        for (int c = nhalf * ncols; c < (nhalf + 1) * ncols; c += 16) {
-          float va[16];
-          if (valid) {
-            kr_pair<16>(prm.after, lin_a, prm.before, lin_b, !prm.mmajor, prm.R, c, prm.vec4 != 0, va);
-          } else {
+      // the thread's 8-column chunks, the loads of a chunk's factor rows issued together
+      for (int c = 8 * part; c < N; c += 32) {
+        float va[8];
+        if (valid) {
+          kr_pair<8>(prm.after, lin_a, prm.before, lin_b, !prm.mmajor, prm.R, c, prm.vec4 != 0, va);
+        } else {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) va[j] = 0.0f;
-          }
-#pragma unroll
-          for (int j = 0; j < 16; ++j) put(c + j, va[j]);
+          for (int j = 0; j < 8; ++j) va[j] = 0.0f;
         }
-      } else {
-        for (int c = nhalf * ncols; c < (nhalf + 1) * ncols; c += 8) {
-          float va[8];
-          if (valid) {
-            kr_pair<8>(prm.after, lin_a, prm.before, lin_b, !prm.mmajor, prm.R, c, prm.vec4 != 0, va);
-          } else {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) va[j] = 0.0f;
-          }
-#pragma unroll
-          for (int j = 0; j < 8; ++j) put(c + j, va[j]);
+        for (int j = 0; j < 8; ++j) {
+          const int n = c + j;
+          const uint32_t off = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128 + ((((k >> 3) ^ (n & 7)) & 7) << 4) +
+                                          (k & 7) * 2);
+          *reinterpret_cast<__nv_bfloat16 *>(kt + off) = __float2bfloat16_rn(va[j]);
         }
       }
       fence_async_smem();
@@ -261,11 +249,11 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
       }
     }
     // ---------------- epilogue: TMEM -> partials ----------------
-    const bool have = (nkb > 0) && mbar_wait_lim(done, 0, abort_flag, prm.spin) && !*abort_flag;
+    const bool have = drains && (nkb > 0) && mbar_wait_lim(done, 0, abort_flag, prm.spin) && !*abort_flag;
     tc_fence_after();
     const int quarter = warp & 3;
     const int row = quarter * 32 + lane;
-    for (int m = 0; m < nqt; ++m) {
+    for (int m = 0; drains && m < nqt; ++m) {
       const int64_t q = (int64_t)(qt0 + m) * TC_BM + row;
       float *dst = prm.partial + ((int64_t)split * prm.Q + q) * N;
       for (int c0 = 0; c0 < N; c0 += 16) {

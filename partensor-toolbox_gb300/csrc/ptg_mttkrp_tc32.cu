@@ -39,6 +39,11 @@ constexpr int T3_KSTAGES = 2;                  // Khatri-Rao ring: [hi rows; lo 
 constexpr int T3_TILE = T3_BM * T3_BK * 4;     // 16 KB
 constexpr int T3_THREADS = 320;
 constexpr uint32_t kTf32HiMask = 0xFFFFE000u;
+// K-blocks one CTA accumulates into its TMEM accumulator.  The accumulation drifts low by a
+// small relative amount per chained MMA, so the chain is cut into splits of at most this many
+// K-blocks (2048 terms); the split-K partials are summed in FP32 in split order, which is
+// unbiased.  At 1000^3 this makes ~500 splits instead of one per SM: 63 MB more partials.
+constexpr int64_t T3_CHAIN_KBLOCKS = 64;
 
 struct T3Params {
   int64_t P, Q, S;
@@ -451,9 +456,11 @@ int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction
     prm.kblocks_total = c.S * prm.pblocks;
   }
   int64_t nsplit = std::max<int64_t>(1, ctx->sm_count / qgroups);
+  nsplit = std::max<int64_t>(nsplit, (prm.kblocks_total + T3_CHAIN_KBLOCKS - 1) / T3_CHAIN_KBLOCKS);
   nsplit = std::min<int64_t>(nsplit, prm.kblocks_total);
   prm.kblocks_per_split = (prm.kblocks_total + nsplit - 1) / nsplit;
   nsplit = (prm.kblocks_total + prm.kblocks_per_split - 1) / prm.kblocks_per_split;
+  if (nsplit > 65535) return set_error(PTG_ERR_UNSUPPORTED, "tensor-core FP32 MTTKRP: too many K-splits");
 
   // tensor map over the FP32 tensor
   CUtensorMap map;

@@ -397,7 +397,8 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
     }
   }
   // ---- learned warm start: features of each row, network inference, logging ----
-  if (a.theta || a.log_X) {
+  if (a.theta || a.log_X) {   // uniform over the CTA
+    __syncthreads();          // Z~ is complete: the choice of start below reads it
     const int Din = R + 8, H = a.hidden;
     const float Lf = (float)np->L;
     float feat[8];
@@ -467,11 +468,43 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
           for (int b = 0; b < RB; ++b)
             if (colok[b]) y[b] = fmaf(__ldg(W3 + (size_t)(lane + 32 * b) * H + u), hu, y[b]);
         }
+        // the row starts from the network's guess only where it has the lower proximal
+        // objective phi(y) = y.Z~y / 2 - W~.y than the reference's own start, the previous
+        // row (include/NesterovMNLS.hpp:200-205): the learned start can only improve it
+        float yn[RB], zn[RB], zp[RB];
 #pragma unroll
         for (int b = 0; b < RB; ++b) {
-          const float st = colok[b] ? fmaxf(y[b] * sc / Lf, 0.0f) : 0.0f;
-          Y[j][b] = st;
-          Ac[j][b] = st;
+          yn[b] = colok[b] ? fmaxf(y[b] * sc / Lf, 0.0f) : 0.0f;
+          zn[b] = 0.0f;
+          zp[b] = 0.0f;
+        }
+        for (int k = 0; k < R; ++k) {
+          const float vn = __shfl_sync(0xffffffffu, (k >> 5) == 0 ? yn[0] : yn[RB - 1], k & 31);
+          const float vp = __shfl_sync(0xffffffffu, (k >> 5) == 0 ? Ac[j][0] : Ac[j][RB - 1], k & 31);
+#pragma unroll
+          for (int b = 0; b < RB; ++b)
+            if (colok[b]) {
+              const float z = Zt[k * R + lane + 32 * b];   // Z~ is symmetric: row k, column c
+              zn[b] = fmaf(z, vn, zn[b]);
+              zp[b] = fmaf(z, vp, zp[b]);
+            }
+        }
+        float pn = 0.0f, pp = 0.0f;
+#pragma unroll
+        for (int b = 0; b < RB; ++b) {
+          pn = fmaf(yn[b], fmaf(0.5f, zn[b], -Wt[j][b]), pn);
+          pp = fmaf(Ac[j][b], fmaf(0.5f, zp[b], -Wt[j][b]), pp);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+          pn += __shfl_xor_sync(0xffffffffu, pn, o);
+          pp += __shfl_xor_sync(0xffffffffu, pp, o);
+        }
+        if (pn < pp) {
+#pragma unroll
+          for (int b = 0; b < RB; ++b) {
+            Y[j][b] = yn[b];
+            Ac[j][b] = yn[b];
+          }
         }
       }
     }

@@ -313,3 +313,23 @@ def test_eigen_bounds_hard_z(pkg, ctx, case):
     for k in range(3):
         err = np.linalg.norm(st.factors[k] - ref.factors[k]) / np.linalg.norm(ref.factors[k])
         assert err < bar, (k, err)
+
+
+def test_dimtree_order5_mixed_constraints_matches_direct(pkg, ctx):
+    """Order 5: the tree splits [0,5) -> [0,3) [3,5) -> [0,2) [2,3) ..., so modes 0 and 1 come
+    from a node recomputed from its parent (include/DimTrees.hpp:862-928).  With an
+    unconstrained and an orthogonal mode among nonnegative ones, cpdDimTree follows the
+    direct cpd per sweep (the same algorithm, another summation order) and the oracle."""
+    dims, R = (9, 8, 7, 6, 5), 3
+    X, init = _nway_problem(dims, R, 77)
+    cons = [pkg.UNCONSTRAINED, pkg.NONNEGATIVITY, pkg.ORTHOGONALITY, pkg.NONNEGATIVITY, pkg.NONNEGATIVITY]
+    o = pkg.Options(order=5, max_iter=6, constraints=cons)
+    st_t = pkg.cpdDimTree(X, R, o, init, ctx=ctx)
+    st_d = pkg.cpd(X, R, o, init, ctx=ctx)
+    ref = oc.cpd_als(X, R, oc.Options(order=5, max_iter=6, constraints=cons), init)
+    rel_t = np.array([t["rel"] for t in st_t.trace])
+    rel_d = np.array([t["rel"] for t in st_d.trace])
+    rel_r = np.array([s["rel"] for s in ref.trace])
+    assert st_t.ao_iter == st_d.ao_iter == ref.ao_iter
+    assert np.max(np.abs(rel_t - rel_d)) < 1e-5, (rel_t, rel_d)
+    assert np.max(np.abs(rel_t - rel_r)) < 1e-4, (rel_t, rel_r)

@@ -63,3 +63,24 @@ def test_cpd_fp32_tensor_cores_follows_oracle(pkg, ctx):
     rel_gpu = np.array([t["rel"] for t in st.trace])
     rel_ref = np.array([s["rel"] for s in ref.trace])
     assert np.max(np.abs(rel_gpu - rel_ref)) < 1e-4
+
+
+def test_mttkrp_fp32_tensor_cores_long_contraction(pkg, ctx):
+    """10^6 terms per output (mode 0 of 64 x 1000 x 1000, the contraction length of the
+    1000^3 modes), uniform [0, 1) data and factors, so that a one-signed drift of the
+    accumulation cannot cancel.  The TMEM accumulation drifts low by ~2^-25 per accumulate
+    step; with each CTA's chain capped at 64 K-blocks (512 steps) the measured error is a
+    -1.9e-5 relative bias (it was ~-5e-5 uncapped).  The bound stated for this opt-in form:
+    3e-5 relative, all of it bias; the CUDA-core FP32 kernel stays the automatic choice."""
+    rng = np.random.default_rng(11)
+    dims, R = (64, 1000, 1000), 32
+    X = rng.random(dims)
+    f = [rng.random((I, R)) for I in dims]
+    for mode in (0, 1):
+        got = _run(pkg, ctx, X, f, R, mode, impl="tensor_cores")
+        ref = oc.mttkrp(f, X, mode)
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        bias = float(np.mean((got - ref) / ref))
+        assert err < 3e-5 and -3e-5 < bias < 1e-6, (mode, err, bias)
+        simt = _run(pkg, ctx, X, f, R, mode, impl="cuda_cores")
+        assert np.linalg.norm(simt - ref) / np.linalg.norm(ref) < 1e-5, mode
