@@ -132,6 +132,13 @@ class Context:
         one fails with PTG_ERR_OOM."""
         check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_ALLOC_LIMIT, int(nbytes)))
 
+    def set_host_read(self, mode: str):
+        """How a host FP64 source reaches the conversion kernels: "auto" (read in place where
+        the device can address the buffer: page-locked memory, or pageable memory where the
+        device walks the host's page tables) or "staged" (copied through device chunks).
+        Both store the same bits."""
+        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_HOST_READ, {"auto": 0, "staged": 1}[mode]))
+
     def enable_stats(self, on: bool = True):
         check(self._lib.ptg_ctx_enable_stats(self.handle, int(on)))
 

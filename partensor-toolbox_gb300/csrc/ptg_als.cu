@@ -516,7 +516,7 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
         logged = off;
       } else {
         for (int n = 0; n < N; ++n) {
-          run.warm[n].theta = mlp_theta(model);
+          run.warm[n].theta = mlp_theta_infer(model, S);
           run.warm[n].hidden = mlp_hidden(model);
         }
       }

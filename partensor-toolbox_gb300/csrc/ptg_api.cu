@@ -251,6 +251,13 @@ int ptg_ctx_create(int device, ptg_ctx **out) {
   c->cc_major = prop.major;
   c->cc_minor = prop.minor;
   c->smem_optin = prop.sharedMemPerBlockOptin;
+  int pageable = 0, host_tables = 0;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) {
+    pageable = host_tables = 0;
+    cudaGetLastError();
+  }
+  c->pageable_ats = pageable == 1 && host_tables == 1;
   cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
@@ -330,6 +337,10 @@ int ptg_ctx_set_option(ptg_ctx *c, int option, long long value) {
       if (value < 0) return set_error(PTG_ERR_INVALID, "allocation limit must be >= 0");
       c->alloc_limit = value;
       return PTG_OK;
+    case PTG_OPT_HOST_READ:
+      if (value != 0 && value != 1) return set_error(PTG_ERR_INVALID, "host read must be 0 (auto) or 1 (staged)");
+      c->host_read = (int)value;
+      return PTG_OK;
     default:
       return set_error(PTG_ERR_INVALID, "unknown option");
   }
@@ -385,6 +396,22 @@ int ptg_tensor_create(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtyp
 
 namespace ptg {
 
+// A device address through which the kernels of context c can read the host buffer src in
+// place, or nullptr where they cannot (the source is then staged through device chunks):
+// page-locked or registered memory by its mapped device pointer, and pageable memory where
+// the device reads through the host's page tables.  Nothing here pins, registers or migrates.
+static const double *host_device_view(ptg_ctx *c, const double *src) {
+  if (c->host_read == 1) return nullptr;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, src) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeHost) return static_cast<const double *>(a.devicePointer);
+  if (a.type == cudaMemoryTypeUnregistered && c->pageable_ats) return src;
+  return nullptr;
+}
+
 int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dtype, const double *src,
                        int src_on_device, DevBuf *storage, ptg_tensor **out, DevBuf *storage32,
                        ptg_tensor **out32) {
@@ -405,6 +432,12 @@ int tensor_create_impl(ptg_ctx *c, int order, const int64_t *dims, ptg_dtype dty
     numel *= dims[k];
   }
   PTG_CUDA(cudaSetDevice(c->device));
+  if (!src_on_device) {   // a host source the kernels can address is read in one pass, in place
+    if (const double *view = host_device_view(c, src)) {
+      src = view;
+      src_on_device = 1;
+    }
+  }
   ptg_tensor *t = new ptg_tensor();
   t->order = order;
   for (int k = 0; k < order; ++k) t->dims[k] = dims[k];

@@ -76,6 +76,10 @@ struct ptg_ctx {
   int *dev_err = nullptr;             // device error word written by bounded waits
   long long spin_limit = -1;          // PTG_OPT_SPIN_LIMIT (-1: the kernels' default)
   long long alloc_limit = 0;          // PTG_OPT_ALLOC_LIMIT (0: none)
+  int host_read = 0;                  // PTG_OPT_HOST_READ
+  // the device reads pageable host memory through the host's page tables (address translation
+  // over NVLink-C2C on Grace; no page migration)
+  bool pageable_ats = false;
   void *f8_work = nullptr;            // FP8 MTTKRP: column-maxima work words + column scales
   std::map<std::string, int> tuned;   // autotuner choices (batched CPD split-K target)
   // buffers of the one-call entry points (ptg_cpd, ptg_cpd_dimtree), kept between calls:
@@ -178,6 +182,9 @@ int simt_mttkrp_fixed_scratch(const ptg_tensor *t, const Contraction &c, int R, 
 
 // Warm-start network accessors (ptg_mlp.cu).
 const float *mlp_theta(const ptg_mlp *m);
+// the weights transposed for the inference fused into the NNLS kernel, refreshed on `s` when
+// training or ptg_mlp_set_params changed them
+const float *mlp_theta_infer(ptg_mlp *m, cudaStream_t s);
 int mlp_din(const ptg_mlp *m);
 int mlp_hidden(const ptg_mlp *m);
 

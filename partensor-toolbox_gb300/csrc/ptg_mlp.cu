@@ -262,6 +262,8 @@ struct ptg_mlp {
   int rank = 0, din = 0, hidden = 0, dout = 0;
   ptg::MlpDims d{};
   float *theta = nullptr, *m = nullptr, *v = nullptr;
+  float *theta_t = nullptr;   // the weights transposed for the fused inference
+  bool t_dirty = true;        // theta changed since theta_t was made
   int adam_t = 0;
   int device = 0;
 };
@@ -269,7 +271,38 @@ struct ptg_mlp {
 using namespace ptg;
 
 namespace ptg {
+namespace {
+// theta_t: W1^T [Din][H], b1, W2^T [H][H], b2, W3^T [H][Dout], b3 (same offsets as theta), so
+// that the inference fused into the NNLS kernel, with one hidden unit or output per lane,
+// reads each weight row of a step as one coalesced line.
+__global__ void mlp_transpose_kernel(const float *__restrict__ th, float *__restrict__ tt, MlpDims d, int din, int h,
+                                     int dout) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < d.n; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t dst = i;
+    if (i >= d.oW1 && i < d.ob1) {          // W1 [h][din] -> [din][h]
+      const int64_t u = (i - d.oW1) / din, j = (i - d.oW1) % din;
+      dst = d.oW1 + j * h + u;
+    } else if (i >= d.oW2 && i < d.ob2) {   // W2 [h][h] -> transposed
+      const int64_t u = (i - d.oW2) / h, j = (i - d.oW2) % h;
+      dst = d.oW2 + j * h + u;
+    } else if (i >= d.oW3 && i < d.ob3) {   // W3 [dout][h] -> [h][dout]
+      const int64_t o = (i - d.oW3) / h, j = (i - d.oW3) % h;
+      dst = d.oW3 + j * dout + o;
+    }
+    tt[dst] = th[i];
+  }
+}
+}  // namespace
+
 const float *mlp_theta(const ptg_mlp *m) { return m->theta; }
+
+const float *mlp_theta_infer(ptg_mlp *m, cudaStream_t s) {
+  if (m->t_dirty) {
+    mlp_transpose_kernel<<<64, 256, 0, s>>>(m->theta, m->theta_t, m->d, m->din, m->hidden, m->dout);
+    m->t_dirty = false;
+  }
+  return m->theta_t;
+}
 int mlp_din(const ptg_mlp *m) { return m->din; }
 int mlp_hidden(const ptg_mlp *m) { return m->hidden; }
 }  // namespace ptg
@@ -288,13 +321,14 @@ int ptg_mlp_create(ptg_ctx *ctx, int rank, unsigned long long seed, ptg_mlp **ou
   m->dout = rank;
   m->d = mlp_dims(m->din, m->hidden, m->dout);
   m->device = ctx->device;
-  cudaError_t e = cudaMalloc(&m->theta, sizeof(float) * 3 * m->d.n);
+  cudaError_t e = cudaMalloc(&m->theta, sizeof(float) * 4 * m->d.n);
   if (e != cudaSuccess) {
     delete m;
     return cuda_error(e, "cudaMalloc(MLP)", __FILE__, __LINE__);
   }
   m->m = m->theta + m->d.n;
   m->v = m->m + m->d.n;
+  m->theta_t = m->v + m->d.n;
   cudaMemsetAsync(m->m, 0, sizeof(float) * 2 * m->d.n, ctx->stream);
   mlp_init_kernel<<<64, 256, 0, ctx->stream>>>(m->theta, m->din, m->hidden, m->dout, seed);
   count_launches(ctx, 1);
@@ -324,6 +358,7 @@ int ptg_mlp_get_params(ptg_ctx *ctx, const ptg_mlp *m, float *host_out) {
 int ptg_mlp_set_params(ptg_ctx *ctx, ptg_mlp *m, const float *host_in) {
   if (!ctx || !m || !host_in) return set_error(PTG_ERR_INVALID, "NULL argument");
   PTG_CUDA(cudaMemcpyAsync(m->theta, host_in, sizeof(float) * m->d.n, cudaMemcpyHostToDevice, ctx->stream));
+  m->t_dirty = true;
   PTG_CUDA(cudaMemsetAsync(m->m, 0, sizeof(float) * 2 * m->d.n, ctx->stream));
   m->adam_t = 0;
   PTG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -425,6 +460,7 @@ int ptg_mlp_train(ptg_ctx *ctx, ptg_mlp *m, const float *X_dev, const float *T_d
     mlp_adam_kernel<<<(int)((m->d.n + 255) / 256), 256, 0, ctx->stream>>>(aa);
     count_launches(ctx, 3);
   }
+  if (steps > 0) m->t_dirty = true;
   std::vector<double> h(nctas, 0.0);
   e = cudaGetLastError();
   if (e == cudaSuccess && steps > 0)

@@ -428,6 +428,8 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
         if (lane < 8) a.log_X[(size_t)i * Din + R + lane] = feat[lane];
       }
       if (a.theta && i < I) {   // uniform per warp: i depends on the warp only
+        // theta is the transposed copy (mlp_theta_infer): W1^T [Din][H], b1, W2^T [H][H], b2,
+        // W3^T [H][R], b3, so every step below reads one contiguous weight row across the lanes
         const float *W1 = a.theta, *b1 = W1 + (size_t)H * Din, *W2 = b1 + H, *b2 = W2 + (size_t)H * H;
         const float *W3 = b2 + H, *b3 = W3 + (size_t)R * H;
         float h1[4], h2[4];
@@ -437,13 +439,13 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
           const float xj = __shfl_sync(0xffffffffu, (jj >> 5) == 0 ? x[0] : x[RB - 1], jj & 31);
 #pragma unroll
           for (int q = 0; q < 4; ++q)
-            if (lane + 32 * q < H) h1[q] = fmaf(__ldg(W1 + (size_t)(lane + 32 * q) * Din + jj), xj, h1[q]);
+            if (lane + 32 * q < H) h1[q] = fmaf(__ldg(W1 + (size_t)jj * H + lane + 32 * q), xj, h1[q]);
         }
 #pragma unroll
         for (int t = 0; t < 8; ++t)
 #pragma unroll
           for (int q = 0; q < 4; ++q)
-            if (lane + 32 * q < H) h1[q] = fmaf(__ldg(W1 + (size_t)(lane + 32 * q) * Din + R + t), feat[t], h1[q]);
+            if (lane + 32 * q < H) h1[q] = fmaf(__ldg(W1 + (size_t)(R + t) * H + lane + 32 * q), feat[t], h1[q]);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           h1[q] = fmaxf(h1[q], 0.0f);
@@ -454,7 +456,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
           const float hv = __shfl_sync(0xffffffffu, qv == 0 ? h1[0] : qv == 1 ? h1[1] : qv == 2 ? h1[2] : h1[3], v & 31);
 #pragma unroll
           for (int q = 0; q < 4; ++q)
-            if (lane + 32 * q < H) h2[q] = fmaf(__ldg(W2 + (size_t)(lane + 32 * q) * H + v), hv, h2[q]);
+            if (lane + 32 * q < H) h2[q] = fmaf(__ldg(W2 + (size_t)v * H + lane + 32 * q), hv, h2[q]);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) h2[q] = fmaxf(h2[q], 0.0f);
@@ -466,7 +468,7 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
           const float hu = __shfl_sync(0xffffffffu, qu == 0 ? h2[0] : qu == 1 ? h2[1] : qu == 2 ? h2[2] : h2[3], u & 31);
 #pragma unroll
           for (int b = 0; b < RB; ++b)
-            if (colok[b]) y[b] = fmaf(__ldg(W3 + (size_t)(lane + 32 * b) * H + u), hu, y[b]);
+            if (colok[b]) y[b] = fmaf(__ldg(W3 + (size_t)u * R + lane + 32 * b), hu, y[b]);
         }
         // the row starts from the network's guess only where it has the lower proximal
         // objective phi(y) = y.Z~y / 2 - W~.y than the reference's own start, the previous

@@ -1,7 +1,9 @@
 """GPU parity of FP8 (e4m3, per-slab scales) tensor storage and its tcgen05 MTTKRP.
 
-* The stored codes and slab scales are bit-exact against oracle/fp8.py, for host and device
-  sources (stochastic rounding from a hash of each entry's position).
+* The stored codes and slab scales are bit-exact against oracle/fp8.py, for device sources
+  and for host sources read in place (pageable memory where the device walks the host's page
+  tables, page-locked memory) or staged through device chunks (stochastic rounding from a
+  hash of each entry's position).
 * The MTTKRP matches ``oracle.fp8.mttkrp`` -- the same FP8 codes and the same two-part
   e4m3 Khatri-Rao operand, summed in FP64 -- within 2e-5 relative (Frobenius): only the
   FP32 accumulation order of the MMA and of the split-K sum differs.
@@ -51,12 +53,20 @@ def _tensor(rng, dims, scale_per_slab=True):
 
 
 @pytest.mark.parametrize("dims", [(23, 19, 17), (40, 48, 56), (16, 9, 5, 7), (130, 3, 6), (5, 4, 3)])
-@pytest.mark.parametrize("source", ["host", "device"])
+@pytest.mark.parametrize("source", ["host", "host_staged", "pinned", "device"])
 def test_fp8_encode_bit_exact(pkg, ctx, dims, source):
     rng = np.random.default_rng(sum(dims))
     X = _tensor(rng, dims)
-    if source == "host":
-        T = pkg.Tensor(ctx, np.asfortranarray(X), precision="fp8")
+    if source in ("host", "host_staged"):
+        ctx.set_host_read("staged" if source == "host_staged" else "auto")
+        try:
+            T = pkg.Tensor(ctx, np.asfortranarray(X), precision="fp8")
+        finally:
+            ctx.set_host_read("auto")
+    elif source == "pinned":
+        host = torch.empty(X.size, dtype=torch.float64, pin_memory=True)
+        host.numpy()[:] = X.reshape(-1, order="F")
+        T = pkg.Tensor(ctx, host.numpy(), dims=dims, precision="fp8")
     else:
         dev = torch.tensor(X.reshape(-1, order="F"), dtype=torch.float64, device="cuda:0")
         T = pkg.Tensor(ctx, (dev.data_ptr(), dims), precision="fp8")
