@@ -247,7 +247,13 @@ def run_ours(args):
     torch.cuda.empty_cache()
     max_iter = args.max_iter
 
+    model = None
+
     def solve(form, tgt=target):
+        if form == "bf16_warm":
+            o = pkg.Options(order=3, max_iter=max_iter, threshold_error=tgt, precision="bf16", verify_fp32=True,
+                            warm_start=True, warm_model=model, warm_log_sweeps=0)
+            return pkg.cpd_resident(ctx, Xb, R, o, init, refine=Xf)
         if form in ("bf16", "fp8"):
             o = pkg.Options(order=3, max_iter=max_iter, threshold_error=tgt, precision=form, verify_fp32=True)
             return pkg.cpd_resident(ctx, Xb if form == "bf16" else X8, R, o, init, refine=Xf)
@@ -290,6 +296,44 @@ def run_ours(args):
     ms_b = _max_over_ranks(ms_b, ws)
     ms_8 = _max_over_ranks(ms_8, ws)
     ms_f = _max_over_ranks(ms_f, ws)
+
+    # BF16 + the learned warm start: the network is trained on every sweep of 12-sweep BF16
+    # solves of instances of the same family drawn on the device (other seeds), then used from
+    # sweep 1 of the headline solve
+    warm = None
+    if not args.no_warm:
+        from partensor_toolbox_gb300 import datagen as dg
+        model = pkg.WarmStartModel(ctx, R, seed=7)
+        t_train = time.perf_counter()
+        for s_ in range(args.warm_train_instances):
+            q = dg.make_cpd_problem(dims, R, seed=1000 + s_, snr_db=SNR_DB, equalize_columns=True, device="cuda")
+            Xq = pkg.Tensor(ctx, (q.X.data_ptr(), dims), precision="bf16")
+            init_q = [f.cpu().numpy() for f in q.init_factors]
+            del q
+            torch.cuda.empty_cache()
+            pkg.cpd_resident(ctx, Xq, R, pkg.Options(order=3, max_iter=12, threshold_error=0.0, precision="bf16",
+                                                     warm_start=True, warm_model=model, warm_log_sweeps=12,
+                                                     warm_train_steps=600), init_q)
+            Xq.close()
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t_train
+        solve("bf16_warm")
+        ms_w, st_w, _ = timed("bf16_warm", max(1, args.steps_plain))
+        last_w = st_w[-1]
+        its = lambda st: sum(sum(t["nesterov_iters"]) for t in st.trace)
+        warm = {"value": _max_over_ranks(ms_w, ws) / 1e3, "unit": "s", "sweeps": last_w.ao_iter,
+                "final_rel_err": last_w.rel_costFunction, "converged": bool(last_w.rel_costFunction <= target),
+                "nesterov_iters_total": its(last_w), "plain_bf16_nesterov_iters_total": its(st_b[-1]),
+                "rel_after_sweep": [round(t["rel"], 5) for t in last_w.trace][:6],
+                "plain_bf16_rel_after_sweep": [round(t["rel"], 5) for t in st_b[-1].trace][:6],
+                "training": {"instances": args.warm_train_instances, "sweeps_logged_each": 12, "adam_steps": 600,
+                             "seconds": round(t_train, 2)},
+                "note": "every row subproblem hits the 50-iteration cap in every sweep, plain or warm, so "
+                        "the start cannot save inner iterations here; the network's start lowers the fit "
+                        "early and then slows the outer convergence",
+                "vs_plain_fp32": (ms_f / ms_w) if ms_w > 0 else None}
+        model.close()
+        model = None
 
     peak, peak_kind = _peaks()
 
@@ -346,13 +390,27 @@ def run_ours(args):
             pkg.cpd(hnp, R, o, init, dims=dims, ctx=ctx)
             tss.append(time.perf_counter() - t)
         ctx.set_host_read("auto")
+        # the host link's own rate: the copy engine moving the same page-locked buffer to HBM
+        link = []
+        dst = torch.empty(p.X.size, dtype=torch.float64, device="cuda")
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            dst.copy_(host, non_blocking=True)
+            torch.cuda.synchronize()
+            link.append(hnp.nbytes / (time.perf_counter() - t) / 1e9)
+        del dst
+        torch.cuda.empty_cache()
+        link_gbs = max(link)
         e2e = {"value": _max_over_ranks(statistics.mean(ts), ws), "unit": "s",
                "h2d_bytes_per_step": int(hnp.nbytes + sum(f.nbytes for f in init)),
                "d2h_bytes_per_step": int(sum(f.nbytes for f in st_e.factors)),
                "rel_err": st_e.rel_costFunction, "min": min(ts), "median": statistics.median(ts),
                "calls_s": [round(x, 5) for x in ts],
                "host_read": "in place (page-locked buffer read by the conversion kernels)",
-               "staged_calls_s": [round(x, 5) for x in tss]}
+               "staged_calls_s": [round(x, 5) for x in tss],
+               "h2d_link_GBs": round(link_gbs, 1),
+               "link_floor_s": hnp.nbytes / (link_gbs * 1e9) + ms_b / 1e3}
         del host
 
     sweeps64 = fp64_sweeps_to(fx, target)
@@ -397,6 +455,7 @@ def run_ours(args):
                                          "final_rel_err": st_fs[-1].rel_costFunction,
                                          "converged": bool(st_fs[-1].rel_costFunction <= strict)}},
         "speedup_vs_plain_fp32": (ms_f / ms_b) if ms_b > 0 else None,
+        "warm_start": warm,
         "speedup_fp8_vs_plain_fp32": (ms_f / ms_8) if ms_8 > 0 else None,
         "roofline": roof_b,
         "gpu_launches": kst["launches"],
@@ -838,6 +897,8 @@ def main():
     ap.add_argument("--steps-e2e", type=int, default=5)
     ap.add_argument("--max-iter", type=int, default=200)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-warm", action="store_true", help="skip the BF16 + learned warm start entry")
+    ap.add_argument("--warm-train-instances", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--warmup-ref", type=int, default=0)
     ap.add_argument("--workload", default="cpd-1000",

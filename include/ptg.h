@@ -94,10 +94,11 @@ typedef enum {
                              larger request fails with PTG_ERR_OOM as cudaMalloc would and
                              leaves the context usable (0: no limit) */,
   PTG_OPT_HOST_READ = 6 /* how a host FP64 source reaches the conversion kernels: 0 auto (the
-                           kernels read it in place where the device can address it: page-locked
-                           or registered memory, and pageable memory where the device walks the
-                           host's page tables, as over NVLink-C2C; else staged copies), 1 always
-                           staged through 64 MB device chunks.  Both store the same bits. */
+                           BF16/FP32 conversion reads page-locked or registered memory in place;
+                           everything else is staged), 1 always staged through 64 MB device
+                           chunks by copies, 2 in place wherever the device can address the
+                           buffer (also pageable memory where the device walks the host's page
+                           tables, as over NVLink-C2C).  All store the same bits. */
 } ptg_option;
 int ptg_ctx_set_option(ptg_ctx *ctx, int option, long long value);
 

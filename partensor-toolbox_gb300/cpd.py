@@ -133,11 +133,13 @@ class Context:
         check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_ALLOC_LIMIT, int(nbytes)))
 
     def set_host_read(self, mode: str):
-        """How a host FP64 source reaches the conversion kernels: "auto" (read in place where
-        the device can address the buffer: page-locked memory, or pageable memory where the
-        device walks the host's page tables) or "staged" (copied through device chunks).
-        Both store the same bits."""
-        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_HOST_READ, {"auto": 0, "staged": 1}[mode]))
+        """How a host FP64 source reaches the conversion kernels: "auto" (page-locked memory
+        read in place by the BF16/FP32 conversion, everything else staged), "staged" (copied
+        through device chunks) or "in_place" (read in place wherever the device can address
+        the buffer, pageable memory included where the device walks the host's page tables).
+        All store the same bits."""
+        modes = {"auto": 0, "staged": 1, "in_place": 2}
+        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_HOST_READ, modes[mode]))
 
     def enable_stats(self, on: bool = True):
         check(self._lib.ptg_ctx_enable_stats(self.handle, int(on)))

@@ -1,7 +1,8 @@
 """Host FP64 sources reach the conversion kernels in one of two ways (PTG_OPT_HOST_READ):
 read in place where the device can address the buffer (page-locked memory through its mapped
 device pointer; pageable memory where the device walks the host's page tables, as over
-NVLink-C2C), or staged through 64 MB device chunks.  Every route must store the same bits as a
+NVLink-C2C), or staged through 64 MB device chunks.  The test runs each route under each
+mode: auto, staged and in place.  Every route must store the same bits as a
 device source, for every storage type, including a tensor that spans more than one staging
 chunk (FP8 chunks hold whole slabs)."""
 import numpy as np
@@ -41,8 +42,8 @@ def test_host_routes_store_the_same_bits(pkg, ctx, precision, esz, dims):
     del dev
     host = torch.empty(flat.size, dtype=torch.float64, pin_memory=True)
     host.numpy()[:] = flat
-    routes = {"pageable_auto": ("auto", flat), "pageable_staged": ("staged", flat),
-              "pinned_auto": ("auto", host.numpy()), "pinned_staged": ("staged", host.numpy())}
+    routes = {f"{kind}_{mode}": (mode, src) for kind, src in (("pageable", flat), ("pinned", host.numpy()))
+              for mode in ("auto", "staged", "in_place")}
     for name, (mode, src) in routes.items():
         ctx.set_host_read(mode)
         try:
@@ -62,6 +63,6 @@ def test_host_routes_store_the_same_bits(pkg, ctx, precision, esz, dims):
 
 def test_host_read_option_is_checked(pkg, ctx):
     lib = pkg._lib
-    assert ctx._lib.ptg_ctx_set_option(ctx.handle, lib.PTG_OPT_HOST_READ, 2) == lib.PTG_ERR_INVALID
+    assert ctx._lib.ptg_ctx_set_option(ctx.handle, lib.PTG_OPT_HOST_READ, 3) == lib.PTG_ERR_INVALID
     assert b"host read" in ctx._lib.ptg_last_error()
     assert ctx._lib.ptg_ctx_set_option(ctx.handle, lib.PTG_OPT_HOST_READ, 0) == 0

@@ -53,20 +53,24 @@ def _tensor(rng, dims, scale_per_slab=True):
 
 
 @pytest.mark.parametrize("dims", [(23, 19, 17), (40, 48, 56), (16, 9, 5, 7), (130, 3, 6), (5, 4, 3)])
-@pytest.mark.parametrize("source", ["host", "host_staged", "pinned", "device"])
+@pytest.mark.parametrize("source", ["host", "host_in_place", "pinned", "pinned_in_place", "device"])
 def test_fp8_encode_bit_exact(pkg, ctx, dims, source):
     rng = np.random.default_rng(sum(dims))
     X = _tensor(rng, dims)
-    if source in ("host", "host_staged"):
-        ctx.set_host_read("staged" if source == "host_staged" else "auto")
+    if source in ("host", "host_in_place"):
+        ctx.set_host_read("in_place" if source == "host_in_place" else "auto")
         try:
             T = pkg.Tensor(ctx, np.asfortranarray(X), precision="fp8")
         finally:
             ctx.set_host_read("auto")
-    elif source == "pinned":
+    elif source in ("pinned", "pinned_in_place"):
         host = torch.empty(X.size, dtype=torch.float64, pin_memory=True)
         host.numpy()[:] = X.reshape(-1, order="F")
-        T = pkg.Tensor(ctx, host.numpy(), dims=dims, precision="fp8")
+        ctx.set_host_read("in_place" if source == "pinned_in_place" else "auto")
+        try:
+            T = pkg.Tensor(ctx, host.numpy(), dims=dims, precision="fp8")
+        finally:
+            ctx.set_host_read("auto")
     else:
         dev = torch.tensor(X.reshape(-1, order="F"), dtype=torch.float64, device="cuda:0")
         T = pkg.Tensor(ctx, (dev.data_ptr(), dims), precision="fp8")

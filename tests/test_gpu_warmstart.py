@@ -1,8 +1,12 @@
 """GPU tests of the learned NNLS warm start (ptg_mlp_*): the network's forward pass and
-gradient against the FP64 oracle (oracle/mlp.py), training on the GPU, and a warm-started
-CPD that must reach the same fit as the plain one.  The effect on the inner Nesterov
-iterations is measured and returned, not assumed (the reference's own start -- the
-previous factor -- is hard to beat late in ALS)."""
+gradient against the FP64 oracle (oracle/mlp.py), training on the GPU, a warm-started CPD
+that must reach the same fit as the plain one, and the gain of a network trained on earlier
+instances of a problem family: on new instances of a 4-way collinear family, at the
+reference's Nesterov tolerance (1e-2) with line-search acceleration on, the warm-started
+solves must need at least 20 % fewer sweeps and inner iterations in total than the plain
+ones, every one reaching the same target.  (Where every row subproblem hits the 50-iteration
+cap in every sweep, as at 1000^3 R=32, no start can save iterations; the bench reports that
+case beside the headline.)"""
 import numpy as np
 import pytest
 import torch
@@ -73,6 +77,8 @@ def test_training_reduces_loss(pkg, ctx):
 
 
 def _collinear_problem(dims, R, seed, snr_db=25.0, cos=0.6):
+    """Factors U[0,1] mixed with one shared column (expected cosine ~cos), Gaussian noise at
+    snr_db; returns the tensor, U[0,1] initial factors and ||noise|| / ||X||."""
     rng = np.random.default_rng(seed)
     A = []
     for I in dims:
@@ -80,16 +86,17 @@ def _collinear_problem(dims, R, seed, snr_db=25.0, cos=0.6):
         c = rng.random((I, 1))
         A.append((1 - cos) * U + cos * c)
     X = np.einsum("ir,jr,kr,lr->ijkl", *A)
-    X = X + np.sqrt((X ** 2).mean() / 10 ** (snr_db / 10)) * rng.standard_normal(dims)
+    noise = np.sqrt((X ** 2).mean() / 10 ** (snr_db / 10)) * rng.standard_normal(dims)
+    X = X + noise
     init = [rng.random((I, R)) for I in dims]
-    return X, init
+    return X, init, float(np.linalg.norm(noise) / np.linalg.norm(X))
 
 
 def warm_vs_plain(pkg, ctx, delta=10.0):
     """Same dimension-tree CPD with and without the learned warm start (log sweeps 1-5,
     train, infer from sweep 6).  Returns both statuses."""
     dims, R = (40, 40, 40, 40), 8
-    X, init = _collinear_problem(dims, R, seed=3)
+    X, init, _ = _collinear_problem(dims, R, seed=3)
     base = dict(order=4, max_iter=12, nesterov_delta_1=delta, nesterov_delta_2=delta, acceleration=False)
     plain = pkg.cpdDimTree(X, R, pkg.Options(**base), init, ctx=ctx)
     model = pkg.WarmStartModel(ctx, R, seed=7)
@@ -110,3 +117,33 @@ def test_warm_start_keeps_the_fit_and_reports_iterations(pkg, ctx):
     it_plain = sum(sum(t["nesterov_iters"]) for t in plain.trace[5:])
     it_warm = sum(sum(t["nesterov_iters"]) for t in warm.trace[5:])
     print(f"inner Nesterov iterations in sweeps 6-12: plain {it_plain}, warm start {it_warm}")
+
+
+def test_network_trained_on_a_family_saves_sweeps_and_iterations(pkg, ctx):
+    """Train on every sweep of 12-sweep solves of four instances, then solve six new instances
+    of the family from sweep 1 with the network, against the plain solver from the same
+    initial factors: reference tolerance, acceleration on, stop at noise floor + 1e-3."""
+    dims, R, delta = (30, 30, 30, 30), 8, 1e-2
+    model = pkg.WarmStartModel(ctx, R, seed=7)
+    for s in range(4):
+        X, init, _ = _collinear_problem(dims, R, seed=100 + s)
+        pkg.cpdDimTree(X, R, pkg.Options(order=4, max_iter=12, threshold_error=0.0, nesterov_delta_1=delta,
+                                         nesterov_delta_2=delta, warm_start=True, warm_model=model,
+                                         warm_log_sweeps=12, warm_train_steps=400), init, ctx=ctx)
+    sweeps = {"plain": 0, "warm": 0}
+    inner = {"plain": 0, "warm": 0}
+    for s in range(4, 10):
+        X, init, nr = _collinear_problem(dims, R, seed=100 + s)
+        base = dict(order=4, max_iter=100, threshold_error=nr + 1e-3, nesterov_delta_1=delta,
+                    nesterov_delta_2=delta)
+        runs = {"plain": pkg.cpdDimTree(X, R, pkg.Options(**base), init, ctx=ctx),
+                "warm": pkg.cpdDimTree(X, R, pkg.Options(**base, warm_start=True, warm_model=model,
+                                                         warm_log_sweeps=0), init, ctx=ctx)}
+        for k, st in runs.items():
+            assert st.ao_iter < 100 and st.rel_costFunction < nr + 1e-3, (k, s, st.ao_iter, st.rel_costFunction)
+            sweeps[k] += st.ao_iter
+            inner[k] += sum(sum(t["nesterov_iters"]) for t in st.trace)
+    print(f"sweeps plain {sweeps['plain']} warm {sweeps['warm']}; inner iterations plain {inner['plain']} "
+          f"warm {inner['warm']}")
+    assert sweeps["warm"] <= 0.8 * sweeps["plain"], sweeps
+    assert inner["warm"] <= 0.8 * inner["plain"], inner
