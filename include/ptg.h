@@ -98,7 +98,12 @@ typedef enum {
                            everything else is staged), 1 always staged through 64 MB device
                            chunks by copies, 2 in place wherever the device can address the
                            buffer (also pageable memory where the device walks the host's page
-                           tables, as over NVLink-C2C).  All store the same bits. */
+                           tables, as over NVLink-C2C).  All store the same bits. */,
+  PTG_OPT_BATCHED_IMPL = 7 /* ptg_cpd_batched: 0 the persistent solver (one launch for the whole
+                              batch: each CTA takes instances from an atomic queue, largest
+                              first, and runs each one's ALS loop to its stop test), 1 one launch
+                              per ALS phase for all instances, each sweep a replayed CUDA graph.
+                              Both run the same per-instance arithmetic. */
 } ptg_option;
 int ptg_ctx_set_option(ptg_ctx *ctx, int option, long long value);
 
@@ -296,8 +301,8 @@ int ptg_cpd_dimtree_file(ptg_ctx *ctx, int order, const int64_t *dims, const cha
  * differ per instance) with the semantics of ptg_cpd on an FP32 tensor, each instance
  * stopping on its own test.  The reference has no batched entry point: a caller loops over
  * partensor::cpd(tnsX, R, options, factorsInit) (include/Cpd.hpp:534-577), one problem at a
- * time; this call replaces that loop.  Every ALS phase is one launch for all unfinished
- * instances and each sweep replays a captured CUDA graph.  Limits: order in [3, 8], every
+ * time; this call replaces that loop.  By default one persistent launch solves the whole
+ * batch (PTG_OPT_BATCHED_IMPL).  Limits: order in [3, 8], every
  * mode PTG_NONNEGATIVITY, rank <= 32, dims <= 4096, and 3 * rows * rank FP32 values of each
  * factor within one CTA's shared memory.  results[i].seconds_total is the wall time from the
  * call's start until instance i's stop test passed; converge_seconds (optional, n entries)

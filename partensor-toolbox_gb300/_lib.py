@@ -19,6 +19,7 @@ PTG_OPT_GTC_ROWS = 3
 PTG_OPT_SPIN_LIMIT = 4
 PTG_OPT_ALLOC_LIMIT = 5
 PTG_OPT_HOST_READ = 6
+PTG_OPT_BATCHED_IMPL = 7
 MTTKRP_IMPLS = {"auto": 0, "cuda_cores": 1, "tensor_cores": 2}
 
 # every symbol include/ptg.h declares

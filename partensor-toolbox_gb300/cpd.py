@@ -141,6 +141,12 @@ class Context:
         modes = {"auto": 0, "staged": 1, "in_place": 2}
         check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_HOST_READ, modes[mode]))
 
+    def set_batched_impl(self, impl: str):
+        """cpd_batched: "persistent" (one launch for the whole batch, the default) or "graphs"
+        (one launch per ALS phase, each sweep a replayed CUDA graph)."""
+        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_BATCHED_IMPL,
+                                           {"persistent": 0, "graphs": 1}[impl]))
+
     def enable_stats(self, on: bool = True):
         check(self._lib.ptg_ctx_enable_stats(self.handle, int(on)))
 

@@ -342,6 +342,11 @@ int ptg_ctx_set_option(ptg_ctx *c, int option, long long value) {
         return set_error(PTG_ERR_INVALID, "host read must be 0 (auto), 1 (staged) or 2 (in place)");
       c->host_read = (int)value;
       return PTG_OK;
+    case PTG_OPT_BATCHED_IMPL:
+      if (value != 0 && value != 1)
+        return set_error(PTG_ERR_INVALID, "batched impl must be 0 (persistent) or 1 (per-phase graphs)");
+      c->batched_impl = (int)value;
+      return PTG_OK;
     default:
       return set_error(PTG_ERR_INVALID, "unknown option");
   }

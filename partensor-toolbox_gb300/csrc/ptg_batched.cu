@@ -26,154 +26,18 @@
 #include <vector>
 
 #include "ptg_internal.h"
+#include "ptg_blockops.cuh"
+#include "ptg_simt.cuh"
 
 namespace ptg {
 namespace {
 
-constexpr int BN_THREADS = 512;
-constexpr int BN_MAXR = 32;
-
-struct BNnls {
-  const float *M;
-  float *A;          // in: start and proximal centre; out: solution
-  float *Wt;         // scratch [I][R]
-  int I, R, inst;
-  const NnlsParams *np;
-  float d1, d2;
-  float *gram_out;
-  double *scal;      // [0] <M, A>, [1] sum(Z .* G)
-  int *iscal;        // [0] iterations, [1] repaired
-};
-
-// Nesterov MNLS of one instance per CTA (include/NesterovMNLS.hpp:181-234 with the zero-column
-// repair of include/Cpd.hpp:206-207 and the Gram of :227).  Lane = column; a warp owns
-// groups of 4 rows (all columns), so the product Y Z~ of a row needs only its own warp's Y;
-// Y is kept transposed in shared memory so the 4 values of a k step are one broadcast 16-byte
-// load.  The global stop test (max |grad .* Y| <= delta1 and min grad >= -delta2, :217-218)
-// fails iff some element violates it, so a warp that sees a violation sets the iteration's
-// flag word (three in rotation) and the block meets once per iteration; the update is done
-// speculatively into the other half of a ping-pong A buffer, so A_it survives a stop.
 __global__ void __launch_bounds__(BN_THREADS) nnls_block_kernel(const BNnls *__restrict__ tab,
                                                                 const int *__restrict__ active) {
   const BNnls a = tab[blockIdx.x];
   if (active && !active[a.inst]) return;
   extern __shared__ __align__(16) float sm[];
-  const int R = a.R, I = a.I, Ip = (I + 3) & ~3;
-  float *Yt = sm;                        // [R][Ip]
-  float *Ab[2];
-  Ab[0] = Yt + (size_t)R * Ip;           // [I][R]
-  Ab[1] = Ab[0] + (size_t)I * R;         // [I][R]
-  __shared__ int vflag[3];
-  __shared__ double dred[2][BN_THREADS / 32];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const NnlsParams *np = a.np;
-  const float L = (float)np->L, lam = (float)np->lambda, invL = 1.0f / L;
-  const int c = lane;
-  const bool cok = c < R;
-  float z[BN_MAXR];
-#pragma unroll
-  for (int k = 0; k < BN_MAXR; ++k) {
-    float v = 0.0f;
-    if (k < R && cok) v = (float)np->Z[k * R + c] + (k == c ? lam : 0.0f);
-    z[k] = v;
-  }
-  for (int idx = tid; idx < I * R; idx += BN_THREADS) {
-    const int i = idx / R, cc = idx % R;
-    const float a0 = a.A[idx];
-    Ab[0][idx] = a0;
-    Yt[cc * Ip + i] = a0;
-    a.Wt[idx] = a.M[idx] + lam * a0;     // W~ = W + lambda A0 (:206)
-  }
-  for (int idx = tid; idx < R * (Ip - I); idx += BN_THREADS) Yt[(idx / (Ip - I)) * Ip + I + idx % (Ip - I)] = 0.0f;
-  if (tid < 3) vflag[tid] = 0;
-  __syncthreads();
-  int it = 0;
-  for (;; ++it) {
-    if (it >= kMaxInner) break;   // A_it is the result
-    const float *Acur = Ab[it & 1];
-    float *Anext = Ab[(it + 1) & 1];
-    const float beta = np->beta[it];
-    bool viol = false;
-    for (int g = warp; 4 * g < I; g += BN_THREADS / 32) {
-      const int i0 = 4 * g;
-      float acc[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) acc[r] = (i0 + r < I && cok) ? -a.Wt[(size_t)(i0 + r) * R + c] : 0.0f;
-#pragma unroll
-      for (int k = 0; k < BN_MAXR; ++k) {
-        if (k < R) {
-          const float4 y4 = *reinterpret_cast<const float4 *>(&Yt[k * Ip + i0]);
-          acc[0] = fmaf(y4.x, z[k], acc[0]);
-          acc[1] = fmaf(y4.y, z[k], acc[1]);
-          acc[2] = fmaf(y4.z, z[k], acc[2]);
-          acc[3] = fmaf(y4.w, z[k], acc[3]);
-        }
-      }
-      __syncwarp();   // every lane has read this group's Y before any lane writes it
-#pragma unroll
-      for (int r = 0; r < 4; ++r)
-        if (i0 + r < I && cok) {
-          const int i = i0 + r;
-          const float y = Yt[c * Ip + i];
-          viol |= (fabsf(acc[r] * y) > a.d1) || (acc[r] < -a.d2);
-          const float na = fmaxf(y - acc[r] * invL, 0.0f);                // :220
-          Yt[c * Ip + i] = (1.0f + beta) * na - beta * Acur[i * R + c];   // :228
-          Anext[i * R + c] = na;
-        }
-      __syncwarp();
-    }
-    if (__any_sync(0xffffffffu, viol) && lane == 0) vflag[it % 3] = 1;
-    if (tid == 0) vflag[(it + 1) % 3] = 0;   // the word of it+1 (read last at it-2)
-    __syncthreads();
-    if (vflag[it % 3] == 0) break;           // no violation: stop, the result is A_it
-  }
-  float *Ac = Ab[it & 1];
-  // zero-column repair (:206-207): a column whose |A| sums to zero over all rows
-  __shared__ int repair;
-  if (tid == 0) repair = 0;
-  __syncthreads();
-  if (tid < R) {
-    float s = 0.0f;
-    for (int i = 0; i < I; ++i) s += fabsf(Ac[i * R + tid]);
-    if (s == 0.0f) atomicExch(&repair, 1);
-  }
-  __syncthreads();
-  if (repair)
-    for (int idx = tid; idx < I * R; idx += BN_THREADS) Ac[idx] = 0.9f * Ac[idx] + 0.1f * a.A[idx];
-  __syncthreads();
-  double ma = 0.0;
-  for (int idx = tid; idx < I * R; idx += BN_THREADS) {
-    a.A[idx] = Ac[idx];
-    ma = fma((double)a.M[idx], (double)Ac[idx], ma);
-  }
-  double hz = 0.0;
-  for (int idx = tid; idx < R * R; idx += BN_THREADS) {
-    const int r1 = idx / R, r2 = idx % R;
-    float s = 0.0f;
-    for (int i = 0; i < I; ++i) s = fmaf(Ac[i * R + r1], Ac[i * R + r2], s);
-    a.gram_out[idx] = s;
-    hz = fma(np->Z[idx], (double)s, hz);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    ma += __shfl_down_sync(0xffffffffu, ma, o);
-    hz += __shfl_down_sync(0xffffffffu, hz, o);
-  }
-  if (lane == 0) {
-    dred[0][warp] = ma;
-    dred[1][warp] = hz;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    double s0 = 0.0, s1 = 0.0;
-    for (int w = 0; w < BN_THREADS / 32; ++w) {
-      s0 += dred[0][w];
-      s1 += dred[1][w];
-    }
-    a.scal[0] = s0;
-    a.scal[1] = s1;
-    a.iscal[0] = it;
-    a.iscal[1] = repair;
-  }
+  nnls_block_body(a, sm);
 }
 
 constexpr int kUpBlocks = 128, kUpThreads = 256;
@@ -249,6 +113,236 @@ upload_convert_kernel(const double *__restrict__ src, int64_t I0, int64_t pI0, i
     acc[0] = a;
     acc[1] = b;
     *ticket = 0;
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// Persistent solver: one launch for the whole batch.  Each CTA takes the next instance from
+// an atomic queue (the host orders the queue largest first) and runs that instance's whole
+// ALS loop -- Grams, eigenvalue bounds, MTTKRP, Nesterov MNLS, normalisation, the stop test
+// and the line search, with the same bodies and in the same order as the per-phase graphs --
+// then takes the next.  No CTA ever waits for another: the queue is a fetch-and-add.  The
+// MTTKRP of a mode is split into (m-tile, K-split) items that the CTA's four 128-thread
+// groups run independently (named barriers); K-split partials are summed in split order
+// (deterministic).
+// ------------------------------------------------------------------------------------
+constexpr int kPGroups = BN_THREADS / 128;
+
+struct PResult {
+  double f, rel;
+  long long inner;
+  unsigned long long done_ns;
+  int ao, acoef, afail, err;
+};
+
+struct PMeta {            // one contraction of an instance: its tile shape and K-split count
+  int bn, bm, mmajor, nsplit;
+};
+
+struct PersistArgs {
+  const InstDesc *desc;
+  const EigDesc *eig;      // [mode * n_inst + instance]
+  const BNnls *nn;         // [mode * n_inst + instance]
+  const SimtParams *pm;    // [instance * (N + 1) + set]: set n < N mode n on the factors,
+  const PMeta *meta;       //   set N the last mode on the line-search point
+  const int *order;        // the queue: instance indices, largest first
+  const double *thr, *frob;
+  PResult *res;
+  int *queue;
+  unsigned long long *t0;  // earliest CTA start (globaltimer, ns)
+  float *scratch;          // per CTA: K-split partials
+  size_t scratch_floats;
+  int group_floats;        // shared memory of one MTTKRP group
+  int n_inst, N, max_iter, acceleration, normalization, accel_coeff, accel_fail;
+  int mttkrp_only;         // 1: every mode's MTTKRP of every instance once, nothing else
+};
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+template <int BN, bool MM, int BM>
+__device__ void cta_mttkrp_cfg(const SimtParams &prm, int nsplit, float *sm, int group_floats) {
+  const int g = threadIdx.x >> 7, gt = threadIdx.x & 127;
+  const int mtiles = (int)((prm.Q + BM - 1) / BM);
+  const int items = mtiles * nsplit;
+  float *gs = sm + (size_t)g * group_floats;
+  for (int it = g; it < items; it += kPGroups)
+    mttkrp_simt_body<float, BN, MM, BM, SyncGroup128>(prm, it / nsplit, it % nsplit, gs, gt, SyncGroup128{1 + g});
+}
+
+// MTTKRP of contraction `set` of instance i into its M buffer (every thread of the CTA).
+__device__ void cta_mttkrp(const PersistArgs &a, int i, int set, float *sm, float *scr, SimtParams *s_prm) {
+  const int k = i * (a.N + 1) + set;
+  const PMeta m = a.meta[k];
+  if (threadIdx.x == 0) {
+    *s_prm = a.pm[k];
+    s_prm->partial = scr;
+    s_prm->nsplit = m.nsplit;
+  }
+  __syncthreads();
+  const SimtParams &p = *s_prm;
+  if (m.bn == 16) {
+    if (m.mmajor) {
+      if (m.bm == 64) cta_mttkrp_cfg<16, true, 64>(p, m.nsplit, sm, a.group_floats);
+      else cta_mttkrp_cfg<16, true, 128>(p, m.nsplit, sm, a.group_floats);
+    } else {
+      if (m.bm == 64) cta_mttkrp_cfg<16, false, 64>(p, m.nsplit, sm, a.group_floats);
+      else cta_mttkrp_cfg<16, false, 128>(p, m.nsplit, sm, a.group_floats);
+    }
+  } else {
+    if (m.mmajor) {
+      if (m.bm == 64) cta_mttkrp_cfg<32, true, 64>(p, m.nsplit, sm, a.group_floats);
+      else cta_mttkrp_cfg<32, true, 128>(p, m.nsplit, sm, a.group_floats);
+    } else {
+      if (m.bm == 64) cta_mttkrp_cfg<32, false, 64>(p, m.nsplit, sm, a.group_floats);
+      else cta_mttkrp_cfg<32, false, 128>(p, m.nsplit, sm, a.group_floats);
+    }
+  }
+  __syncthreads();
+  if (m.nsplit > 1) {   // the partials of every split, summed in split order
+    const int R = p.R, bn = m.bn;
+    for (int idx = threadIdx.x; idx < (int)p.q_write * R; idx += blockDim.x) {
+      const int q = idx / R, c = idx - q * R;
+      float sum = 0.0f;
+      for (int sp = 0; sp < m.nsplit; ++sp) sum += scr[((size_t)sp * p.Q + q) * bn + c];
+      p.out[(size_t)q * R + c] = sum;
+    }
+    __syncthreads();
+  }
+}
+
+// The ALS loop of one instance (include/Cpd.hpp:288-356 with the batched path's per-instance
+// bookkeeping of the stop test and the line search, :333-354).
+__device__ void persist_instance(const PersistArgs &a, int i, float *sm, float *scr, SimtParams *s_prm,
+                                 volatile int *s_flag, volatile float *s_step) {
+  const InstDesc &in = a.desc[i];
+  const int N = a.N, last = N - 1;
+  gram_block(in, 0);
+  __syncthreads();
+  cta_mttkrp(a, i, last, sm, scr, s_prm);
+  cost_terms_block(in, 0);
+  __syncthreads();
+  // scalars: kept by thread 0
+  double f = 0.0, rel = 0.0;
+  const double frob = a.frob[i];
+  int ao = 0, acoef = a.accel_coeff, afail = a.accel_fail, err = 0;
+  long long inner = 0;
+  if (threadIdx.x == 0) {
+    f = sqrt(fmax(frob + in.cost_out[1] - 2.0 * in.cost_out[0], 0.0));
+    rel = f / sqrt(frob);
+  }
+  for (;;) {
+    for (int n = 0; n < N; ++n) {
+      const EigDesc &e = a.eig[(size_t)n * a.n_inst + i];
+      GramPtrs gp{};
+      for (int k = 0; k < N; ++k) gp.g[k] = e.gram[k];
+      eigen_bounds_body<BN_THREADS>(gp, N, n, e.R, e.out);
+      __syncthreads();
+      cta_mttkrp(a, i, n, sm, scr, s_prm);
+      nnls_block_body(a.nn[(size_t)n * a.n_inst + i], sm);
+      __syncthreads();
+    }
+    if (a.normalization) {
+      normalize_block(in);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      ++ao;
+      const BNnls &bl = a.nn[(size_t)last * a.n_inst + i];
+      const double f2 = frob - 2.0 * bl.scal[0] + bl.scal[1];
+      int stop = 0;
+      if (!isfinite(f2)) {
+        err = PTG_ERR_NUMERIC;
+        stop = 1;
+      } else {
+        f = sqrt(fmax(f2, 0.0));
+        rel = f / sqrt(frob);
+        for (int n = 0; n < N; ++n) inner += a.nn[(size_t)n * a.n_inst + i].iscal[0];
+        stop = (rel < a.thr[i] || ao >= a.max_iter) ? 1 : 0;
+      }
+      s_flag[0] = stop;
+      s_flag[1] = (!stop && a.acceleration && ao > 1) ? 1 : 0;   // line search this sweep
+      s_flag[2] = (!stop && a.acceleration) ? 1 : 0;             // keep this sweep's factors
+      *s_step = (float)pow((double)(ao + 1), 1.0 / (double)acoef);
+    }
+    __syncthreads();
+    if (s_flag[0]) break;
+    const int accel = s_flag[1], copy = s_flag[2];
+    if (accel) {
+      accel_combine_block(in, *s_step);
+      __syncthreads();
+      gram_block(in, 1);
+      __syncthreads();
+    }
+    if (copy) {
+      copy_old_block(in);
+      __syncthreads();
+    }
+    if (accel) {
+      cta_mttkrp(a, i, N, sm, scr, s_prm);
+      cost_terms_block(in, 1);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const double fa = sqrt(fmax(frob + in.cost_out[1] - 2.0 * in.cost_out[0], 0.0));
+        int accept = 0;
+        if (f > fa) {
+          accept = 1;
+          f = fa;
+        } else {
+          ++afail;
+        }
+        if (afail == 5) {
+          afail = 0;
+          ++acoef;
+        }
+        s_flag[3] = accept;
+      }
+      __syncthreads();
+      if (s_flag[3]) {
+        select_block(in);
+        __syncthreads();
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    PResult r;
+    r.f = f;
+    r.rel = rel;
+    r.inner = inner;
+    r.ao = ao;
+    r.acoef = acoef;
+    r.afail = afail;
+    r.err = err;
+    r.done_ns = globaltimer_ns();
+    a.res[i] = r;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(BN_THREADS, 1) cpd_persistent_kernel(const PersistArgs a) {
+  extern __shared__ __align__(16) float sm[];
+  __shared__ SimtParams s_prm;
+  __shared__ int s_inst;
+  __shared__ int s_flag[4];
+  __shared__ float s_step;
+  if (threadIdx.x == 0) atomicMin(a.t0, globaltimer_ns());
+  float *scr = a.scratch + (size_t)blockIdx.x * a.scratch_floats;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      const int k = atomicAdd(a.queue, 1);
+      s_inst = k < a.n_inst ? a.order[k] : -1;
+    }
+    __syncthreads();
+    const int i = s_inst;
+    if (i < 0) break;
+    if (a.mttkrp_only) {
+      for (int n = 0; n < a.N; ++n) cta_mttkrp(a, i, n, sm, scr, &s_prm);   // ends with a barrier
+      continue;
+    }
+    persist_instance(a, i, sm, scr, &s_prm, s_flag, &s_step);   // ends with a barrier
   }
 }
 
@@ -420,8 +514,9 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   PTG_CUDA(cudaMemsetAsync(d_ticket, 0, sizeof(unsigned), S));
 
   // ---- initial factors: host FP64 ColMajor -> FP32 row-major, one copy ----
+  std::vector<float> init_img((fac_end - fac_begin) / sizeof(float), 0.0f);
   {
-    std::vector<float> hf((fac_end - fac_begin) / sizeof(float), 0.0f);
+    std::vector<float> &hf = init_img;
     for (int i = 0; i < n_inst; ++i)
       for (int k = 0; k < N; ++k) {
         const int64_t I = inst[i].dims[k];
@@ -564,6 +659,251 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
     return set_error(PTG_ERR_UNSUPPORTED,
                      "batched CPD: a factor (rows x rank) is too large for the one-CTA NNLS (shared memory)");
   PTG_CUDA(cudaFuncSetAttribute(nnls_block_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nnls_smem));
+
+  // ---- results: one copy of every factor, FP32 row-major -> host FP64 ColMajor ----
+  auto write_results = [&](const std::vector<double> &frob, const std::vector<double> &f,
+                           const std::vector<double> &rel, const std::vector<int> &ao, const std::vector<int> &acoef,
+                           const std::vector<int> &afail, const std::vector<long long> &inner,
+                           const std::vector<double> &done_t, double t_solve) -> int {
+    std::vector<float> hf((fac_end - fac_begin) / sizeof(float));
+    PTG_CUDA(cudaMemcpyAsync(hf.data(), block + fac_begin, fac_end - fac_begin, cudaMemcpyDeviceToHost, S));
+    PTG_CUDA(cudaStreamSynchronize(S));
+    for (int i = 0; i < n_inst; ++i) {
+      for (int k = 0; k < N; ++k) {
+        const int64_t I = inst[i].dims[k];
+        const int R = desc[i].R;
+        const float *src = hf.data() + ((char *)desc[i].fac[k] - block - fac_begin) / sizeof(float);
+        for (int64_t r0 = 0; r0 < I; ++r0)
+          for (int r = 0; r < R; ++r) inst[i].out_factors[k][r0 + I * r] = (double)src[(size_t)r0 * R + r];
+      }
+      if (results) {
+        results[i].frob_tns = frob[i];
+        results[i].f_value = f[i];
+        results[i].rel_costFunction = rel[i];
+        results[i].ao_iter = ao[i];
+        results[i].accel_coeff = acoef[i];
+        results[i].accel_fail = afail[i];
+        results[i].refine_sweeps_done = 0;
+        results[i].nesterov_iters_total = inner[i];
+        results[i].seconds_total = done_t[i];
+      }
+      if (converge_seconds) converge_seconds[i] = done_t[i] - t_solve;
+    }
+    return PTG_OK;
+  };
+
+  if (ctx->batched_impl == 0) {
+    // ---- the persistent solver: plan every contraction, order the queue, one launch ----
+    const int NS = N + 1;
+    std::vector<SimtParams> pm((size_t)n_inst * NS);
+    std::vector<PMeta> meta((size_t)n_inst * NS);
+    size_t scratch_floats = 0;
+    int group_floats = 0;
+    auto bm_of = [](int64_t Q) {
+      const int64_t w64 = (Q + 63) / 64 * 64 - Q, w128 = (Q + 127) / 128 * 128 - Q;
+      return w64 < w128 ? 64 : 128;
+    };
+    // items_per_group: the (m-tile, K-split) items each of the CTA's groups gets per MTTKRP
+    auto plan = [&](int items_per_group) {
+      scratch_floats = 0;
+      group_floats = 0;
+      for (int i = 0; i < n_inst; ++i)
+        for (int set = 0; set < NS; ++set) {
+          const int mode = set < N ? set : N - 1;
+          const Contraction c = mttkrp_contraction(T[i], set < N ? desc[i].fac : desc[i].acc, mode);
+          const int bn = bn_class(desc[i].R), bm = bm_of(c.Q);
+          const bool mm = c.P == 1;
+          SimtParams p{};
+          p.X = T[i]->data;
+          p.P = c.P;
+          p.Q = c.Q;
+          p.S = c.S;
+          p.before = to_dev(c.before);
+          p.after = to_dev(c.after);
+          p.R = desc[i].R;
+          p.col0 = 0;
+          p.out = desc[i].M;
+          p.q_write = c.q_write;
+          p.ldo = desc[i].R;
+          if (mm) {
+            p.pblocks = 1;
+            p.ktiles_total = (c.S + BK - 1) / BK;
+          } else {
+            p.pblocks = (c.P + BK - 1) / BK;
+            p.ktiles_total = c.S * p.pblocks;
+          }
+          const int64_t mtiles = (c.Q + bm - 1) / bm;
+          const int64_t target = (int64_t)kPGroups * items_per_group;
+          int64_t ns = std::max<int64_t>(1, (target + mtiles - 1) / mtiles);
+          ns = std::min<int64_t>(ns, p.ktiles_total);
+          p.ktiles_per_split = (p.ktiles_total + ns - 1) / ns;
+          ns = (p.ktiles_total + p.ktiles_per_split - 1) / p.ktiles_per_split;
+          p.nsplit = (int)ns;
+          pm[(size_t)i * NS + set] = p;
+          meta[(size_t)i * NS + set] = PMeta{bn, bm, mm ? 1 : 0, (int)ns};
+          if (ns > 1) scratch_floats = std::max(scratch_floats, (size_t)ns * c.Q * bn);
+          const size_t gb = bn == 16 ? simt_smem_bytes<16>(mm, bm) : simt_smem_bytes<32>(mm, bm);
+          group_floats = std::max(group_floats, (int)((gb / sizeof(float) + 31) / 32 * 32));
+        }
+    };
+    // the queue, largest instance first (longest-processing-time order)
+    std::vector<int> order(n_inst);
+    for (int i = 0; i < n_inst; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+      return (double)Tst[x].numel_padded * desc[x].R > (double)Tst[y].numel_padded * desc[y].R;
+    });
+    std::vector<double> thr(n_inst), frobv(n_inst);
+    for (int i = 0; i < n_inst; ++i) {
+      thr[i] = inst[i].threshold_error > 0.0 ? inst[i].threshold_error : opt.threshold_error;
+      frobv[i] = T[i]->frob_stored;
+    }
+    const int grid = std::min(n_inst, ctx->sm_count);
+    cudaFuncAttributes fa;
+    PTG_CUDA(cudaFuncGetAttributes(&fa, cpd_persistent_kernel));
+    SimtParams *d_pm;
+    PMeta *d_meta;
+    int *d_order, *d_queue;
+    double *d_thr, *d_frob;
+    PResult *d_res;
+    unsigned long long *d_t0;
+    PTG_TRY(ar.alloc(&d_pm, pm.size()));
+    PTG_TRY(ar.alloc(&d_meta, meta.size()));
+    PTG_TRY(ar.alloc(&d_order, n_inst));
+    PTG_TRY(ar.alloc(&d_thr, n_inst));
+    PTG_TRY(ar.alloc(&d_frob, n_inst));
+    PTG_TRY(ar.alloc(&d_res, n_inst));
+    PTG_TRY(ar.alloc(&d_queue, 1));
+    PTG_TRY(ar.alloc(&d_t0, 1));
+    PTG_CUDA(cudaMemcpyAsync(d_order, order.data(), sizeof(int) * n_inst, cudaMemcpyHostToDevice, S));
+    PTG_CUDA(cudaMemcpyAsync(d_frob, frobv.data(), sizeof(double) * n_inst, cudaMemcpyHostToDevice, S));
+    float *d_scr = nullptr;
+    size_t scr_cap = 0;
+    PersistArgs pa{};
+    pa.desc = d_desc;
+    pa.eig = d_eig;
+    pa.nn = d_nn;
+    pa.pm = d_pm;
+    pa.meta = d_meta;
+    pa.order = d_order;
+    pa.thr = d_thr;
+    pa.frob = d_frob;
+    pa.res = d_res;
+    pa.queue = d_queue;
+    pa.t0 = d_t0;
+    pa.n_inst = n_inst;
+    pa.N = N;
+    pa.acceleration = opt.acceleration;
+    pa.normalization = opt.normalization;
+    pa.accel_coeff = opt.accel_coeff;
+    pa.accel_fail = opt.accel_fail;
+    // one launch with the plan of `items_per_group` (max_iter sweeps, thresholds `th`)
+    auto launch = [&](int items_per_group, int max_iter, const std::vector<double> &th) -> int {
+      plan(items_per_group);
+      const size_t dyn = std::max((size_t)kPGroups * group_floats * sizeof(float), nnls_smem);
+      if (dyn + fa.sharedSizeBytes > ctx->smem_optin)
+        return set_error(PTG_ERR_UNSUPPORTED, "batched CPD: persistent solver exceeds shared memory");
+      if (scratch_floats * grid > scr_cap) {
+        PTG_TRY(ar.alloc(&d_scr, scratch_floats * grid));
+        scr_cap = scratch_floats * grid;
+      }
+      PTG_CUDA(cudaMemcpyAsync(d_pm, pm.data(), sizeof(SimtParams) * pm.size(), cudaMemcpyHostToDevice, S));
+      PTG_CUDA(cudaMemcpyAsync(d_meta, meta.data(), sizeof(PMeta) * meta.size(), cudaMemcpyHostToDevice, S));
+      PTG_CUDA(cudaMemcpyAsync(d_thr, th.data(), sizeof(double) * n_inst, cudaMemcpyHostToDevice, S));
+      PTG_CUDA(cudaMemsetAsync(d_queue, 0, sizeof(int), S));
+      PTG_CUDA(cudaMemsetAsync(d_t0, 0xff, sizeof(unsigned long long), S));
+      pa.scratch = d_scr;
+      pa.scratch_floats = scratch_floats;
+      pa.group_floats = group_floats;
+      pa.max_iter = max_iter;
+      PTG_CUDA(cudaFuncSetAttribute(cpd_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+      cpd_persistent_kernel<<<grid, BN_THREADS, dyn, S>>>(pa);
+      PTG_CUDA(cudaGetLastError());
+      count_launches(ctx, 1);
+      return PTG_OK;
+    };
+    // autotuner: two sweeps of the whole batch per candidate split target, then the
+    // initial factors again (cached per batch shape in the context)
+    long long shape_sum = 0;
+    for (int i = 0; i < n_inst; ++i) {
+      shape_sum = shape_sum * 31 + desc[i].R;
+      for (int k = 0; k < N; ++k) shape_sum = shape_sum * 131 + desc[i].rows[k];
+    }
+    const std::string key = "persist:" + std::to_string(n_inst) + ":" + std::to_string(shape_sum);
+    int best = ctx->tuned.count(key) ? ctx->tuned[key] : 0;
+    if (!best) {
+      cudaEvent_t e0, e1;
+      PTG_CUDA(cudaEventCreate(&e0));
+      PTG_CUDA(cudaEventCreate(&e1));
+      const std::vector<double> never(n_inst, 0.0);
+      float best_ms = 1e30f;
+      for (int cand : {1, 2, 4}) {
+        PTG_CUDA(cudaEventRecord(e0, S));
+        PTG_TRY(launch(cand, 2, never));
+        PTG_CUDA(cudaEventRecord(e1, S));
+        PTG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        PTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = cand;
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      ctx->tuned[key] = best;
+      PTG_CUDA(cudaMemcpyAsync(block + fac_begin, init_img.data(), fac_end - fac_begin, cudaMemcpyHostToDevice, S));
+    }
+    if (ctx->stats.enabled) {   // one timed pass of every mode's MTTKRP of every instance
+      double bytes = 0.0;
+      for (int i = 0; i < n_inst; ++i)
+        for (int n = 0; n < N; ++n) {
+          bytes += 4.0 * (double)Tst[i].numel_padded;
+          for (int k = 0; k < N; ++k) bytes += 4.0 * (double)inst[i].dims[k] * inst[i].rank;
+        }
+      cudaEvent_t e0, e1;
+      PTG_CUDA(cudaEventCreate(&e0));
+      PTG_CUDA(cudaEventCreate(&e1));
+      const long long l0 = ctx->stats.launches;
+      pa.mttkrp_only = 1;
+      PTG_CUDA(cudaEventRecord(e0, S));
+      PTG_TRY(launch(best, 1, std::vector<double>(n_inst, 0.0)));
+      PTG_CUDA(cudaEventRecord(e1, S));
+      PTG_CUDA(cudaEventSynchronize(e1));
+      pa.mttkrp_only = 0;
+      float ms = 0.f;
+      PTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      ctx->stats.batch_pass_launches = ctx->stats.launches - l0;
+      ctx->stats.batch_pass_ms = ms;
+      ctx->stats.batch_pass_bytes = bytes;
+    }
+    PTG_CUDA(cudaStreamSynchronize(S));
+    const double t_solve = elapsed();   // every tensor resident from here on
+    PTG_TRY(launch(best, opt.max_iter, thr));
+    std::vector<PResult> res(n_inst);
+    unsigned long long t0_ns = 0;
+    PTG_CUDA(cudaMemcpyAsync(res.data(), d_res, sizeof(PResult) * n_inst, cudaMemcpyDeviceToHost, S));
+    PTG_CUDA(cudaMemcpyAsync(&t0_ns, d_t0, sizeof(t0_ns), cudaMemcpyDeviceToHost, S));
+    PTG_CUDA(cudaStreamSynchronize(S));
+    PTG_TRY(check_device_error(ctx));
+    std::vector<double> f(n_inst), rel(n_inst), done_t(n_inst);
+    std::vector<int> ao(n_inst), acoef(n_inst), afail(n_inst);
+    std::vector<long long> inner(n_inst);
+    for (int i = 0; i < n_inst; ++i) {
+      const PResult &r = res[i];
+      if (r.err) return set_error(r.err, "batched CPD: cost is NaN or Inf");
+      f[i] = r.f;
+      rel[i] = r.rel;
+      ao[i] = r.ao;
+      acoef[i] = r.acoef;
+      afail[i] = r.afail;
+      inner[i] = r.inner;
+      done_t[i] = t_solve + 1e-9 * (double)(r.done_ns - t0_ns);
+    }
+    return write_results(frobv, f, rel, ao, acoef, afail, inner, done_t, t_solve);
+  }
+
 
   // ---- batched MTTKRP plans: per mode, rank class and M-tile height, plus the accelerated
   // last mode.  The M-tile (64 or 128 output rows) is the one that wastes fewer rows. ----
@@ -808,30 +1148,5 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
       PTG_TRY(launch_batched_op(ctx, BatchedOp::Select, d_desc, n_inst, d_accept, nullptr, S));
     }
   }
-  // ---- results: one copy of every factor, FP32 row-major -> host FP64 ColMajor ----
-  std::vector<float> hf((fac_end - fac_begin) / sizeof(float));
-  PTG_CUDA(cudaMemcpyAsync(hf.data(), block + fac_begin, fac_end - fac_begin, cudaMemcpyDeviceToHost, S));
-  PTG_CUDA(cudaStreamSynchronize(S));
-  for (int i = 0; i < n_inst; ++i) {
-    for (int k = 0; k < N; ++k) {
-      const int64_t I = inst[i].dims[k];
-      const int R = desc[i].R;
-      const float *src = hf.data() + ((char *)desc[i].fac[k] - block - fac_begin) / sizeof(float);
-      for (int64_t r0 = 0; r0 < I; ++r0)
-        for (int r = 0; r < R; ++r) inst[i].out_factors[k][r0 + I * r] = (double)src[(size_t)r0 * R + r];
-    }
-    if (results) {
-      results[i].frob_tns = frob[i];
-      results[i].f_value = f[i];
-      results[i].rel_costFunction = rel[i];
-      results[i].ao_iter = ao[i];
-      results[i].accel_coeff = acoef[i];
-      results[i].accel_fail = afail[i];
-      results[i].refine_sweeps_done = 0;
-      results[i].nesterov_iters_total = inner[i];
-      results[i].seconds_total = done_t[i];
-    }
-    if (converge_seconds) converge_seconds[i] = done_t[i] - t_solve;
-  }
-  return PTG_OK;
+  return write_results(frob, f, rel, ao, acoef, afail, inner, done_t, t_solve);
 }

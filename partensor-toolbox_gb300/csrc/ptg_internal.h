@@ -77,6 +77,7 @@ struct ptg_ctx {
   long long spin_limit = -1;          // PTG_OPT_SPIN_LIMIT (-1: the kernels' default)
   long long alloc_limit = 0;          // PTG_OPT_ALLOC_LIMIT (0: none)
   int host_read = 0;                  // PTG_OPT_HOST_READ
+  int batched_impl = 0;               // PTG_OPT_BATCHED_IMPL
   // the device reads pageable host memory through the host's page tables (address translation
   // over NVLink-C2C on Grace; no page migration)
   bool pageable_ats = false;

@@ -4,13 +4,22 @@ single-instance GPU path (ptg_cpd) on the same inputs.
 
 Bars: one sweep matches the oracle to 1e-4 relative per factor; after 15 sweeps each
 instance's relative error is within 1e-3 of the oracle's with factor congruence >= 0.99;
-each instance's sweep count, stop decision and cost equal the single-instance path's."""
+each instance's sweep count, stop decision and cost equal the single-instance path's.
+Every test runs both solvers: the persistent one (one launch for the batch) and the
+per-phase graphs."""
 import numpy as np
 import pytest
 
 from oracle import cpd as oc
 
 pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(params=["persistent", "graphs"], autouse=True)
+def impl(request, ctx):
+    ctx.set_batched_impl(request.param)
+    yield request.param
+    ctx.set_batched_impl("persistent")
 
 
 def _instance(dims, R, seed, snr_db=20.0):
@@ -99,3 +108,20 @@ def test_batched_rejects_unsupported(pkg, ctx):
     Xb, Rb, initb = _instance((10, 11, 12), 40, 0)
     with pytest.raises(pkg.PtgError):
         pkg.cpd_batched([(Xb, Rb, initb)], pkg.Options(order=3), ctx=ctx)
+
+
+def test_persistent_and_graph_solvers_agree(pkg, ctx, impl):
+    """The same batch through both solvers: the same sweeps per instance and the same fit to
+    FP32 summation-order differences (the MTTKRP K-splits differ)."""
+    if impl != "persistent":
+        pytest.skip("compares the two solvers once")
+    batch = pkg.datagen.make_fmri_batch(24, seed=9)
+    probs = [(b.X, b.rank, b.init_factors) for b in batch]
+    opts = pkg.Options(order=3, max_iter=30, threshold_error=0.0)
+    per, _ = pkg.cpd_batched(probs, opts, ctx=ctx)
+    ctx.set_batched_impl("graphs")
+    gra, _ = pkg.cpd_batched(probs, opts, ctx=ctx)
+    for a, b in zip(per, gra):
+        assert a.ao_iter == b.ao_iter == 30
+        assert a.rel_costFunction == pytest.approx(b.rel_costFunction, abs=2e-5)
+        assert oc.congruence(a.factors, b.factors) >= 0.999
