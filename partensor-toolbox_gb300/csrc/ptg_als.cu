@@ -35,7 +35,9 @@ struct AlsBuffers {
   NnlsParams *np = nullptr;
   double *dsc = nullptr;  // [N][2]: <M, A>, sum(Z .* G); [0][2..3]: cost terms of a point;
                           // [4N], [4N + 1]: the line-search decision (accel_select_kernel)
-  int *isc = nullptr;     // [N][2]: iterations, repaired; [2N]: the line search's stop gate
+  int *isc = nullptr;     // [N][2]: iterations, repaired; [2N]: the line search's stop gate;
+                          // [2N + 1]: 1 when the line search took its point (its mode-0
+                          // MTTKRP in M is then the next sweep's)
   double *W = nullptr;    // R x R FP64: Z^{-1} or (M^T M)^{-1/2} (other constraints)
   double *cpart = nullptr;        // launch_cost_terms partials
   unsigned *cticket = nullptr;    // and its ticket (zero between launches)
@@ -114,7 +116,8 @@ struct AlsBuffers {
 // wait for it: the sweep's cost and the accelerated point's cost from their terms (the host's
 // arithmetic in the host's order: the doublings are exact, so contraction cannot change a
 // result), the stop test of the sweep, then acc -> fac and gacc -> gram when the point is
-// taken.  Every block decides alike; block 0 records the point's f^2 and the decision.
+// taken.  Every block decides alike; block 0 records the point's f^2 and the decision, as a
+// double for the host and as an int for the next sweep's mode-0 MTTKRP (Contraction::skip).
 struct SelectArgs {
   const double *dsc;     // sweep terms at [4 last], [4 last + 1]; the point's at [2], [3]
   int last, N, R;
@@ -126,6 +129,7 @@ struct SelectArgs {
   const float *acc[PTG_MAX_ORDER];
   const float *gacc[PTG_MAX_ORDER];
   double *sel;           // out: [0] the point's f^2, [1] 1.0 when taken
+  int *taken;            // out: 1 when taken, else 0
 };
 
 __global__ void accel_select_kernel(const SelectArgs a) {
@@ -139,6 +143,7 @@ __global__ void accel_select_kernel(const SelectArgs a) {
     if (blockIdx.x == 0) {
       a.sel[0] = fa2;
       a.sel[1] = take ? 1.0 : 0.0;
+      *a.taken = take;
     }
   }
   __syncthreads();
@@ -192,8 +197,10 @@ struct Runner {
   }
 
   // the sweep's kernels, then its cost terms, iteration counts and the device error word
-  // copied to pinned memory behind them (ctx->ev_cost); nothing waits
-  int sweep_enqueue(const ptg_tensor *X) {
+  // copied to pinned memory behind them (ctx->ev_cost); nothing waits.  reuse_m0: a device
+  // word that, when nonzero, cancels mode 0's MTTKRP because M already holds it (the line
+  // search before this sweep took its point, whose cost it computed from that product).
+  int sweep_enqueue(const ptg_tensor *X, const int *reuse_m0 = nullptr) {
     cudaStream_t S = ctx->stream, T = ctx->side;
     const int N = b.N, R = b.R;
     if (dimtree) tree.new_sweep();   // normalisation and the line search changed every factor
@@ -212,6 +219,7 @@ struct Runner {
       PTG_CUDA(cudaEventRecord(ctx->ev_join, T));
       if (!dimtree) {
         Contraction c = mttkrp_contraction(X, b.fac, n);
+        if (n == 0) c.skip = reuse_m0;
         PTG_TRY(contraction_launch(ctx, X, c, R, b.M, S));
       } else {
         // through the tree: the nodes on the path to leaf n that a changed factor made stale
@@ -246,17 +254,18 @@ struct Runner {
     return PTG_OK;
   }
 
-  // the line-search point's cost terms (one last-mode MTTKRP in the Gram form) into
-  // b.dsc[2..3], queued
+  // the line-search point's cost terms into b.dsc[2..3], queued, in the Gram form from one
+  // MTTKRP: <X, [[A]]> = <MTTKRP_0(X, A), A_0>, the same cost as the reference's last-mode
+  // form (include/Cpd.hpp:262-266).  Mode 0 because, when the point is taken, that product
+  // (left in b.M) is the next sweep's first MTTKRP, which the sweep then skips.
   int point_cost_enqueue(const ptg_tensor *X, float *const *factors, float *const *grams,
                          const int *skip = nullptr, cudaEvent_t grams_ready = nullptr) {
     cudaStream_t S = ctx->stream;
-    const int last = b.N - 1;
-    Contraction c = mttkrp_contraction(X, factors, last);
+    Contraction c = mttkrp_contraction(X, factors, 0);
     c.skip = skip;
     PTG_TRY(contraction_launch(ctx, X, c, b.R, b.M, S));
     if (grams_ready) PTG_CUDA(cudaStreamWaitEvent(S, grams_ready, 0));
-    PTG_TRY(launch_cost_terms(b.M, factors[last], b.rows[last], grams, b.N, b.R, b.dsc + 2,
+    PTG_TRY(launch_cost_terms(b.M, factors[0], b.rows[0], grams, b.N, b.R, b.dsc + 2,
                               CostScratch{b.cpart, b.cticket}, S));
     count_launches(ctx, 1);
     return PTG_OK;
@@ -285,6 +294,7 @@ struct Runner {
       most = std::max<int64_t>(most, (int64_t)b.rows[k] * b.R);
     }
     a.sel = b.dsc + 4 * b.N;
+    a.taken = b.isc + 2 * b.N + 1;
     const int blocks = (int)std::min<int64_t>((most + 255) / 256, (int64_t)ctx->sm_count);
     accel_select_kernel<<<std::max(blocks, 1), 256, 0, S>>>(a);
     PTG_CUDA(cudaGetLastError());
@@ -332,7 +342,7 @@ struct Runner {
     return PTG_OK;
   }
 
-  // cost of the point (factors, grams) by one last-mode MTTKRP: sqrt(||X||^2 + sum(Z.*G) - 2<M,A>)
+  // cost of the point (factors, grams) by one MTTKRP: sqrt(||X||^2 + sum(Z.*G) - 2<M,A>)
   int point_cost(const ptg_tensor *X, double frob, float *const *factors, float *const *grams,
                  double *f_out) {
     cudaStream_t S = ctx->stream;
@@ -524,8 +534,11 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
     // The sweep, its normalisation and its line search are queued before the host waits for
     // the sweep's cost: the line search's accept decision and the stop test gating it run on
     // the device (accel_select_kernel), and the host reads the decision one sweep later, before
-    // the next line search needs it.  The stream never idles on a host round trip.
-    PTG_TRY(run.sweep_enqueue(Xa));
+    // the next line search needs it.  The stream never idles on a host round trip.  When that
+    // line search took its point, its mode-0 MTTKRP is this sweep's first one (direct
+    // contractions; a tree's nodes would be stale).
+    const bool m0_reusable = sel_pending && !run.dimtree && opt.constraints[0] == PTG_NONNEGATIVITY;
+    PTG_TRY(run.sweep_enqueue(Xa, m0_reusable ? b.isc + 2 * N + 1 : nullptr));
     if (model && ao_iter == log_sweeps && opt.warm_train_steps > 0) {
       double loss = 0.0;
       PTG_TRY(ptg_mlp_train(ctx, model, logX, logT, logged, opt.warm_train_steps, 256, 1e-3f, 1234, &loss));

@@ -144,7 +144,7 @@ struct PersistArgs {
   const EigDesc *eig;      // [mode * n_inst + instance]
   const BNnls *nn;         // [mode * n_inst + instance]
   const SimtParams *pm;    // [instance * (N + 1) + set]: set n < N mode n on the factors,
-  const PMeta *meta;       //   set N the last mode on the line-search point
+  const PMeta *meta;       //   set N mode 0 on the line-search point
   const int *order;        // the queue: instance indices, largest first
   const double *thr, *frob;
   PResult *res;
@@ -230,6 +230,7 @@ __device__ void persist_instance(const PersistArgs &a, int i, float *sm, float *
   const double frob = a.frob[i];
   int ao = 0, acoef = a.accel_coeff, afail = a.accel_fail, err = 0;
   long long inner = 0;
+  int reuse_m0 = 0;   // the last line search took its point: M holds this sweep's mode-0 MTTKRP
   if (threadIdx.x == 0) {
     f = sqrt(fmax(frob + in.cost_out[1] - 2.0 * in.cost_out[0], 0.0));
     rel = f / sqrt(frob);
@@ -241,7 +242,7 @@ __device__ void persist_instance(const PersistArgs &a, int i, float *sm, float *
       for (int k = 0; k < N; ++k) gp.g[k] = e.gram[k];
       eigen_bounds_body<BN_THREADS>(gp, N, n, e.R, e.out);
       __syncthreads();
-      cta_mttkrp(a, i, n, sm, scr, s_prm);
+      if (n != 0 || !reuse_m0) cta_mttkrp(a, i, n, sm, scr, s_prm);
       nnls_block_body(a.nn[(size_t)n * a.n_inst + i], sm);
       __syncthreads();
     }
@@ -271,6 +272,7 @@ __device__ void persist_instance(const PersistArgs &a, int i, float *sm, float *
     __syncthreads();
     if (s_flag[0]) break;
     const int accel = s_flag[1], copy = s_flag[2];
+    reuse_m0 = 0;
     if (accel) {
       accel_combine_block(in, *s_step);
       __syncthreads();
@@ -301,7 +303,8 @@ __device__ void persist_instance(const PersistArgs &a, int i, float *sm, float *
         s_flag[3] = accept;
       }
       __syncthreads();
-      if (s_flag[3]) {
+      reuse_m0 = s_flag[3];
+      if (reuse_m0) {
         select_block(in);
         __syncthreads();
       }
@@ -456,7 +459,7 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
     d_cost = c.take<double>(2 * (size_t)n_inst);
     d_scal = c.take<double>(2 * (size_t)n_inst * N);
     d_iscal = c.take<int>(2 * (size_t)n_inst * N);
-    d_flags = c.take<int>(4 * (size_t)n_inst);
+    d_flags = c.take<int>(5 * (size_t)n_inst);
     d_step = c.take<float>(n_inst);
     d_desc = c.take<InstDesc>(n_inst);
     d_up = c.take<double>(2 * (size_t)n_inst);
@@ -606,17 +609,20 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   PTG_CUDA(cudaMemcpyAsync(d_desc, desc.data(), sizeof(InstDesc) * n_inst, cudaMemcpyHostToDevice, S));
   // flags: active, accelerate, accepted, copy-old; steps
   int *d_active = d_flags, *d_accel = d_flags + n_inst, *d_accept = d_flags + 2 * n_inst, *d_copy = d_flags + 3 * n_inst;
+  // mode 0's MTTKRP runs for active instances whose last line search did not take its point
+  // (a taken point left that product in M)
+  int *d_m0 = d_flags + 4 * n_inst;
   PinnedHost hp;
-  const size_t host_bytes = sizeof(int) * 4 * n_inst + sizeof(float) * n_inst + sizeof(double) * (2 * n_inst * N + 2 * n_inst) +
+  const size_t host_bytes = sizeof(int) * 5 * n_inst + sizeof(float) * n_inst + sizeof(double) * (2 * n_inst * N + 2 * n_inst) +
                             sizeof(int) * 2 * n_inst * N + 16;   // + alignment of the FP64 block
   PTG_CUDA(cudaHostAlloc(&hp.p, host_bytes, cudaHostAllocDefault));
   int *h_flags = (int *)hp.p;
-  float *h_step = (float *)(h_flags + 4 * n_inst);
+  float *h_step = (float *)(h_flags + 5 * n_inst);
   double *h_scal = (double *)(((uintptr_t)(h_step + n_inst) + 7) & ~(uintptr_t)7);
   double *h_cost = h_scal + 2 * n_inst * N;
   int *h_iscal = (int *)(h_cost + 2 * n_inst);
-  for (int i = 0; i < 4 * n_inst; ++i) h_flags[i] = 0;
-  for (int i = 0; i < n_inst; ++i) h_flags[i] = 1;   // all active
+  for (int i = 0; i < 5 * n_inst; ++i) h_flags[i] = 0;
+  for (int i = 0; i < n_inst; ++i) h_flags[i] = h_flags[4 * n_inst + i] = 1;   // all active
 
   // ---- eigen / NNLS descriptors per mode ----
   std::vector<EigDesc> eig((size_t)N * n_inst);
@@ -709,7 +715,7 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
       group_floats = 0;
       for (int i = 0; i < n_inst; ++i)
         for (int set = 0; set < NS; ++set) {
-          const int mode = set < N ? set : N - 1;
+          const int mode = set < N ? set : 0;
           const Contraction c = mttkrp_contraction(T[i], set < N ? desc[i].fac : desc[i].acc, mode);
           const int bn = bn_class(desc[i].R), bm = bm_of(c.Q);
           const bool mm = c.P == 1;
@@ -921,7 +927,7 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   };
   auto build_plans = [&](int target) -> int {
     for (int n = 0; n <= N; ++n) {
-      const int mode = n < N ? n : N - 1;
+      const int mode = n < N ? n : 0;   // the line-search point: mode 0 (the next sweep's first)
       std::map<std::pair<int, int>, std::vector<int>> cls;
       for (int i = 0; i < n_inst; ++i) {
         const Contraction c = mttkrp_contraction(T[i], desc[i].fac, mode);
@@ -1027,7 +1033,7 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
 
   // ---- the sweep as a CUDA graph: for each mode, eigenbounds, MTTKRP, NNLS ----
   GraphHolder sweep_graph, accel_graph;
-  PTG_CUDA(cudaMemcpyAsync(d_flags, h_flags, sizeof(int) * 4 * n_inst, cudaMemcpyHostToDevice, S));
+  PTG_CUDA(cudaMemcpyAsync(d_flags, h_flags, sizeof(int) * 5 * n_inst, cudaMemcpyHostToDevice, S));
   // kernels inside a graph are counted once per replay, not at capture
   long long cap0 = ctx->stats.launches;
   PTG_CUDA(cudaStreamBeginCapture(S, cudaStreamCaptureModeThreadLocal));
@@ -1045,7 +1051,7 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
       fe = cudaEventRecord(side.join, side.s);
       if (fe != cudaSuccess) cap_rc = cuda_error(fe, "graph join", __FILE__, __LINE__);
     }
-    if (cap_rc == PTG_OK) cap_rc = mttkrp_all(n, d_active);
+    if (cap_rc == PTG_OK) cap_rc = mttkrp_all(n, n == 0 ? d_m0 : d_active);
     if (cap_rc == PTG_OK) {
       fe = cudaStreamWaitEvent(S, side.join, 0);
       if (fe != cudaSuccess) cap_rc = cuda_error(fe, "graph join", __FILE__, __LINE__);
@@ -1080,7 +1086,9 @@ extern "C" int ptg_cpd_batched(ptg_ctx *ctx, int n_inst, const ptg_cpd_instance 
   int n_active = n_inst;
   const double t_solve = elapsed();   // every tensor resident from here on
   for (int sweep = 1; n_active > 0; ++sweep) {
+    for (int i = 0; i < n_inst; ++i) h_flags[4 * n_inst + i] = h_flags[i] && !h_flags[2 * n_inst + i];
     PTG_CUDA(cudaMemcpyAsync(d_flags, h_flags, sizeof(int) * n_inst, cudaMemcpyHostToDevice, S));
+    PTG_CUDA(cudaMemcpyAsync(d_m0, h_flags + 4 * n_inst, sizeof(int) * n_inst, cudaMemcpyHostToDevice, S));
     PTG_CUDA(cudaGraphLaunch(sweep_graph.e, S));
     count_launches(ctx, (int)sweep_kernels);
     PTG_CUDA(cudaMemcpyAsync(h_scal, d_scal, sizeof(double) * 2 * n_inst * N, cudaMemcpyDeviceToHost, S));

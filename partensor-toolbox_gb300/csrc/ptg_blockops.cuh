@@ -405,14 +405,16 @@ __device__ void select_block(const InstDesc &in) {
   }
 }
 
-// FP64 cost terms of a point: out[0] = <M, A_last>, out[1] = sum(Z_last .* G_last)
+// FP64 cost terms of a point: out[0] = <M, A_m>, out[1] = sum of the Hadamard product of all
+// Grams, with M the MTTKRP of mode m: the last mode for the factors (the sweep's own), mode 0
+// for the line-search point (its mode-0 MTTKRP is the next sweep's first one when it is taken)
 __device__ void cost_terms_block(const InstDesc &in, int use_acc) {
-  const int last = in.order - 1, R = in.R;
-  const float *A = use_acc ? in.acc[last] : in.fac[last];
+  const int last = in.order - 1, R = in.R, m = use_acc ? 0 : last;
+  const float *A = use_acc ? in.acc[m] : in.fac[m];
   float *const *G = use_acc ? in.gacc : in.gram;
   __shared__ double red[2][32];
   double s = 0.0, h = 0.0;
-  for (int64_t idx = threadIdx.x; idx < (int64_t)in.rows[last] * R; idx += blockDim.x)
+  for (int64_t idx = threadIdx.x; idx < (int64_t)in.rows[m] * R; idx += blockDim.x)
     s = fma((double)in.M[idx], (double)A[idx], s);
   for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
     double z = 1.0;
