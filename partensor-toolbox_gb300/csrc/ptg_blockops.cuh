@@ -37,29 +37,35 @@ __device__ int sturm_count_f32(const float *d, const float *e2, int n, float x) 
   return cnt;
 }
 
-// Same count in FP64 without divisions: the sign changes of the characteristic-polynomial
-// sequence p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}, rescaled by exact powers of two so
-// it neither overflows nor underflows (GB300's FP64 rate is low; a division costs ~10 FMAs).
-__device__ int sturm_count_f64(const double *d, const double *e2, int n, double x) {
+// Sign of p for a Sturm count (0 positive, 1 negative); a zero takes the previous sign.  Read
+// from the high and low words with integer instructions.
+__device__ __forceinline__ int sturm_sign(double p, int prev) {
+  const int hi = __double2hiint(p), lo = __double2loint(p);
+  return (((hi & 0x7fffffff) | lo) == 0) ? prev : (int)((unsigned)hi >> 31);
+}
+
+// The same count in FP64 for a tridiagonal scaled so that its Gershgorin interval lies in
+// [-1, 1]: the sign changes of the characteristic-polynomial sequence
+// p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2} (p_{-1} = 1), a zero taking the previous sign.
+// With |d_i - x| <= 2 and e^2 <= 1, |p| grows by less than a factor 3 per step, so 64 steps
+// cannot overflow; when both of the last two values fall below 2^-600 they are scaled up by
+// 2^600 (exact).  On GB300 a warp's FP64 instruction holds its SM sub-partition for about 64
+// cycles, so a step is three FP64 instructions (subtract, multiply, fused multiply-add) and
+// the sign and range tests run on the integer pipe.
+__device__ int sturm_count_f64s(const double *d, const double *e2, int n, double x) {
   double pm2 = 1.0, pm1 = d[0] - x;
-  int sprev = 1;                                  // sign of p_{-1} = 1
-  int s1 = pm1 < 0.0 ? -1 : (pm1 > 0.0 ? 1 : sprev);
-  int cnt = (s1 != sprev);
-  sprev = s1;
+  int sprev = sturm_sign(pm1, 0);
+  int cnt = sprev;   // p_{-1} = 1 > 0
   for (int i = 1; i < n; ++i) {
-    double p = (d[i] - x) * pm1 - e2[i - 1] * pm2;
-    const int s = p < 0.0 ? -1 : (p > 0.0 ? 1 : sprev);
-    cnt += (s != sprev);
+    const double p = fma(d[i] - x, pm1, -(e2[i - 1] * pm2));
+    const int s = sturm_sign(p, sprev);
+    cnt += s ^ sprev;
     sprev = s;
     pm2 = pm1;
     pm1 = p;
-    const double a = fabs(pm1);
-    if (a > 0x1p+256) {
-      pm1 *= 0x1p-256;
-      pm2 *= 0x1p-256;
-    } else if (a < 0x1p-256 && fabs(pm2) < 0x1p-256) {
-      pm1 *= 0x1p+256;
-      pm2 *= 0x1p+256;
+    if (((__double2hiint(pm1) >> 20) & 0x7ff) < 423 && ((__double2hiint(pm2) >> 20) & 0x7ff) < 423) {
+      pm1 *= 0x1p+600;
+      pm2 *= 0x1p+600;
     }
   }
   return cnt;
@@ -72,7 +78,7 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
   constexpr int lda = kMaxR + 1;              // padded rows: column reads and mirrored writes
   __shared__ double A[kMaxR * lda];           // spread over the banks
   __shared__ double xs[kMaxR], vs[kMaxR], ws[kMaxR];
-  __shared__ double ps[NT / kMaxR][kMaxR];
+  __shared__ double ps[4][kMaxR];
   __shared__ double d[kMaxR], e[kMaxR], e2[kMaxR];
   __shared__ double redb[2][NT / 32];
   __shared__ double s_scalar[4];
@@ -104,10 +110,12 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if ((tid & 31) == 0) redb[rb][tid >> 5] = x;
     __syncthreads();
-    double sum = 0.0;
-    for (int i = 0; i < NT / 32; ++i) sum += redb[rb][i];
+    // every warp sums the partials by a butterfly: the same bits in every lane (each step
+    // adds the same two values), five FP64 additions instead of one per warp
+    double v = (tid & 31) < NT / 32 ? redb[rb][tid & 31] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     rb ^= 1;
-    return sum;
+    return v;
   };
 
   // ---- Householder tridiagonalisation (Golub & Van Loan alg. 8.3.1), H = I - beta v v^T,
@@ -116,7 +124,10 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
   // the square root and the division (one thread: GB300's FP64 pipe is the scarce resource).
   // Thread (q, i) sums a quarter of row i's terms, reading column entries (A is symmetric) so
   // that a warp's threads read consecutive addresses. ----
-  const int pi = tid & (kMaxR - 1), pq = tid / kMaxR;
+  // the product A_sub x: thread (pq, pi) sums a part of row pi's terms; rows in 32 or 64
+  // slots, at most 4 parts (fewer FP64 instructions on the longest thread, and a short sum)
+  const int yrows = n <= 32 ? 32 : kMaxR, yparts = min(NT / yrows, 4);
+  const int pi = tid % yrows, pq = tid / yrows;
   for (int k = 0; k + 2 < n; ++k) {
     const int m = n - k - 1;  // length of the column below the diagonal (= row k right of it)
     const double *rowk = A + k * lda + (k + 1);
@@ -128,14 +139,15 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
       if (tid == 0) e[k] = x0;
       continue;
     }
-    double y = 0.0;       // (A_sub x)_i, partial over j in [16 q, 16 q + 16)
-    if (pi < m) {
+    double y = 0.0;       // (A_sub x)_i, partial over part pq of j
+    if (pi < m && pq < yparts) {
       const double *col = A + (k + 1) * lda + (k + 1 + pi);
-      const int j1 = min(m, (pq + 1) * (kMaxR / (NT / kMaxR)));
-      for (int j = pq * (kMaxR / (NT / kMaxR)); j < j1; ++j) y = fma(col[j * lda], xs[j], y);
+      const int chunk = (m + yparts - 1) / yparts;
+      const int j1 = min(m, (pq + 1) * chunk);
+      for (int j = pq * chunk; j < j1; ++j) y = fma(col[j * lda], xs[j], y);
       ps[pq][pi] = y;
     }
-    if (tid == NT - 1) {   // never holds a row of the product (row 63 > m - 1)
+    if (tid == NT - 1) {   // holds no row of the product (its row slot is past m - 1)
       const double al = (x0 >= 0.0 ? -1.0 : 1.0) * sqrt(x0 * x0 + sigma);
       const double dv = x0 - al;
       s_scalar[0] = al;
@@ -147,7 +159,7 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
     double pv = 0.0, vi = 0.0, pvi = 0.0;
     if (tid < m) {
       double yi = 0.0;
-      for (int q = 0; q < NT / kMaxR; ++q) yi += ps[q][tid];
+      for (int q = 0; q < yparts; ++q) yi += ps[q][tid];
       vi = tid == 0 ? v0 : xi;
       pvi = beta * fma(-alpha, A[(k + 1) * lda + (k + 1 + tid)], yi);   // p_i
       pv = pvi * vi;
@@ -168,60 +180,81 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
     if (tid == 0) e[k] = alpha;
     __syncthreads();
   }
-  if (tid == 0) {
-    for (int i = 0; i < n; ++i) d[i] = A[i * lda + i];
-    if (n >= 2) e[n - 2] = A[(n - 1) * lda + (n - 2)];
-    for (int i = 0; i + 1 < n; ++i) e2[i] = e[i] * e[i];
-    // Gershgorin interval
-    double lo = 1e300, hi = -1e300;
-    for (int i = 0; i < n; ++i) {
+  // ---- T = (d, e) scaled by a power of two, sc, so that its Gershgorin interval lies in
+  // [-1, 1]; the counts and the bisection run on the scaled T (exact), the result is scaled
+  // back at the end ----
+  for (int i = tid; i < n; i += NT) d[i] = A[i * lda + i];
+  if (tid == 0 && n >= 2) e[n - 2] = A[(n - 1) * lda + (n - 2)];
+  __syncthreads();
+  if (tid < 32) {   // warp 0: the Gershgorin interval
+    double glo = 1e300, ghi = -1e300;
+    for (int i = tid; i < n; i += 32) {
       const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < n ? fabs(e[i]) : 0.0);
-      lo = fmin(lo, d[i] - r);
-      hi = fmax(hi, d[i] + r);
+      glo = fmin(glo, d[i] - r);
+      ghi = fmax(ghi, d[i] + r);
     }
-    const double pad = 1e-12 * fmax(fabs(lo), fabs(hi)) + 1e-300;
-    lo -= pad;
-    hi += pad;
-    lohi[0][0] = lo; lohi[0][1] = hi;   // smallest eigenvalue
-    lohi[1][0] = lo; lohi[1][1] = hi;   // largest eigenvalue
-    s_scalar[1] = fmax(fabs(lo), fabs(hi));   // ||T|| bound
-  }
-  __syncthreads();   // d and e2 are complete before any thread reads them (n > 32 spans warps)
-  for (int i = tid; i < n; i += blockDim.x) {
-    df[i] = (float)d[i];
-    e2f[i] = (float)e2[i];
+    for (int o = 16; o > 0; o >>= 1) {
+      glo = fmin(glo, __shfl_xor_sync(0xffffffffu, glo, o));
+      ghi = fmax(ghi, __shfl_xor_sync(0xffffffffu, ghi, o));
+    }
+    if (tid == 0) {
+      const double g = fmax(fabs(glo), fabs(ghi));
+      int E = 0;
+      if (g > 0.0 && isfinite(g)) frexp(g, &E);
+      const double sc = ldexp(1.0, -E);
+      const double gs = g * sc;                     // in [0.5, 1)
+      const double pad = 1e-12 * gs + 1e-300;
+      lohi[0][0] = lohi[1][0] = glo * sc - pad;     // smallest and largest eigenvalue
+      lohi[0][1] = lohi[1][1] = ghi * sc + pad;
+      s_scalar[1] = gs;                             // ||T|| bound, scaled
+      s_scalar[2] = sc;
+    }
   }
   __syncthreads();
+  {
+    const double sc = s_scalar[2];
+    for (int i = tid; i < n; i += NT) {
+      const double di = d[i] * sc;
+      d[i] = di;
+      df[i] = (float)di;
+      if (i + 1 < n) {
+        const double ei = e[i] * sc;
+        e2[i] = ei * ei;
+        e2f[i] = (float)(ei * ei);
+      }
+    }
+  }
+  __syncthreads();   // d and e2 are complete before any thread reads them (n > 32 spans warps)
 
   // ---- bisection: warp 0 brackets the smallest eigenvalue, warp 1 the largest, with a
   // 32-way multisection per round: FP32 counts first, then FP64 counts on the widened
-  // FP32 bracket ----
+  // FP32 bracket.  The points of a round come from fixed fractions (j + 1) / 33 and the new
+  // bracket from two of them (shuffles), so no round divides ----
   if (tid < 64) {
     const int which = tid >> 5;      // 0: min, 1: max
     const int j = tid & 31;
     const int target = which == 0 ? 1 : n;  // count(x) >= target  <=>  x > lambda
-    double lo = lohi[which][0], hi = lohi[which][1];
+    float flo = __double2float_rd(lohi[which][0]), fhi = __double2float_ru(lohi[which][1]);
+    const float cf = (float)(j + 1) * (1.0f / 33.0f);
     for (int round = 0; round < 6; ++round) {
-      const double x = lo + (hi - lo) * (double)(j + 1) / 33.0;
-      const bool hit = sturm_count_f32(df, e2f, n, (float)x) >= target;
+      const float x = fmaf(fhi - flo, cf, flo);
+      const bool hit = sturm_count_f32(df, e2f, n, x) >= target;
       const unsigned m = __ballot_sync(0xffffffffu, hit);
       const int f = m ? (__ffs(m) - 1) : 32;
-      const double nlo = (f == 0) ? lo : lo + (hi - lo) * (double)f / 33.0;
-      const double nhi = (f == 32) ? hi : lo + (hi - lo) * (double)(f + 1) / 33.0;
-      lo = nlo;
-      hi = nhi;
+      const float xl = __shfl_sync(0xffffffffu, x, (f + 31) & 31), xh = __shfl_sync(0xffffffffu, x, f & 31);
+      flo = (f == 0) ? flo : xl;
+      fhi = (f == 32) ? fhi : xh;
     }
     // the FP32 counts are exact for a matrix within a few FP32 ulps of T (entrywise), so
     // the eigenvalue lies within 16 * eps32 * ||T|| of the FP32 bracket
     const double margin = 16.0 * 1.1920929e-7 * s_scalar[1] + 1e-300;
-    lo -= margin;
-    hi += margin;
-    // ... which holds while FP32 represents T well.  Where it does not (entries or their
-    // squares out of FP32 range, or counts off by more than the margin) the FP64 counts at
-    // the widened ends show it: then the FP64 multisection starts over from the Gershgorin
-    // interval, with enough rounds (33^16) to reach FP64 resolution from there.
+    double lo = (double)flo - margin, hi = (double)fhi + margin;
+    // ... which holds while FP32 represents T well.  Where it does not (counts off by more
+    // than the margin) the FP64 counts at the widened ends show it: then the FP64
+    // multisection starts over from the Gershgorin interval, with enough rounds (33^16) to
+    // reach FP64 resolution from there.
     int c_end = 0;
-    if (j < 2) c_end = sturm_count_f64(d, e2, n, j == 0 ? lo : hi);
+    if (j < 2) c_end = sturm_count_f64s(d, e2, n, j == 0 ? lo : hi);
     const int c_lo = __shfl_sync(0xffffffffu, c_end, 0), c_hi = __shfl_sync(0xffffffffu, c_end, 1);
     int rounds64 = 8;
     if (!(c_lo < target && c_hi >= target)) {
@@ -229,15 +262,18 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
       hi = lohi[which][1];
       rounds64 = 16;
     }
+    const double cd = (double)(j + 1) * (1.0 / 33.0);
     for (int round = 0; round < rounds64; ++round) {
-      const double x = lo + (hi - lo) * (double)(j + 1) / 33.0;
-      const bool hit = sturm_count_f64(d, e2, n, x) >= target;
+      // lo and hi are the same in every lane: the warp leaves together once the bracket is
+      // within 2^-42 of the eigenvalue's magnitude
+      if (hi - lo <= 0x1p-42 * fmax(fabs(lo), fabs(hi))) break;
+      const double x = fma(hi - lo, cd, lo);
+      const bool hit = sturm_count_f64s(d, e2, n, x) >= target;
       const unsigned m = __ballot_sync(0xffffffffu, hit);
       const int f = m ? (__ffs(m) - 1) : 32;
-      const double nlo = (f == 0) ? lo : lo + (hi - lo) * (double)f / 33.0;
-      const double nhi = (f == 32) ? hi : lo + (hi - lo) * (double)(f + 1) / 33.0;
-      lo = nlo;
-      hi = nhi;
+      const double xl = __shfl_sync(0xffffffffu, x, (f + 31) & 31), xh = __shfl_sync(0xffffffffu, x, f & 31);
+      lo = (f == 0) ? lo : xl;
+      hi = (f == 32) ? hi : xh;
     }
     if (j == 0) {
       lohi[which][0] = lo;
@@ -245,55 +281,65 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
     }
   }
   __syncthreads();
-  if (tid == 0) {
-    const double lmin = 0.5 * (lohi[0][0] + lohi[0][1]);
-    const double lmax = 0.5 * (lohi[1][0] + lohi[1][1]);
-    // singular values of a symmetric matrix are |eigenvalues|
-    double L = fmax(fabs(lmax), fabs(lmin));
-    double mu = fabs(lmin);
-    if (n == 1) L = mu = fabs(d[0]);
-    {   // scale-free summaries of Z for the warm-start network
-      double dsum = 0.0, dmin = 1e300, dmax = -1e300;
-      for (int i = 0; i < n; ++i) {
-        const double z = out->Z[i * n + i];
-        dsum += z;
-        dmin = fmin(dmin, z);
-        dmax = fmax(dmax, z);
+  if (tid < 32) {
+    // scale-free summaries of Z for the warm-start network: its diagonal's sum, min and max
+    double dsum = 0.0, dmin = 1e300, dmax = -1e300;
+    for (int i = tid; i < n; i += 32) {
+      const double z = out->Z[i * n + i];
+      dsum += z;
+      dmin = fmin(dmin, z);
+      dmax = fmax(dmax, z);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+      dmin = fmin(dmin, __shfl_xor_sync(0xffffffffu, dmin, o));
+      dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    }
+    if (tid == 0) {
+      const double unscale = 1.0 / s_scalar[2];   // a power of two: exact
+      const double lmin = 0.5 * (lohi[0][0] + lohi[0][1]) * unscale;
+      const double lmax = 0.5 * (lohi[1][0] + lohi[1][1]) * unscale;
+      // singular values of a symmetric matrix are |eigenvalues|
+      double L = fmax(fabs(lmax), fabs(lmin));
+      double mu = fabs(lmin);
+      if (n == 1) L = mu = fabs(d[0] * unscale);
+      {
+        const double Ls = L > 0.0 ? L : 1.0;
+        const float inv = (float)(1.0 / Ls);
+        out->feat[0] = log10f((float)fmin(Ls / fmax(mu, 1e-300), 1e30)) / 6.0f;
+        out->feat[1] = (float)mu * inv;
+        out->feat[2] = (float)(dsum / n) * inv;
+        out->feat[3] = (float)dmin * inv;
+        out->feat[4] = (float)dmax * inv;
+        out->feat[6] = (float)n / 64.0f;
+        out->feat[7] = 1.0f;
       }
-      const double Ls = L > 0.0 ? L : 1.0;
-      out->feat[0] = (float)(log10(Ls / fmax(mu, 1e-300)) / 6.0);
-      out->feat[1] = (float)(mu / Ls);
-      out->feat[2] = (float)(dsum / n / Ls);
-      out->feat[3] = (float)(dmin / Ls);
-      out->feat[4] = (float)(dmax / Ls);
-      out->feat[6] = (float)n / 64.0f;
-      out->feat[7] = 1.0f;
+      // GLambda, include/NesterovMNLS.hpp:75-91
+      double q = mu / L, lam;
+      if (1.0 / q > 1e6) lam = 10.0 * mu;
+      else if (1.0 / q > 1e3) lam = mu;
+      else lam = mu / 10.0;
+      L += lam;
+      mu += lam;
+      q = mu / L;
+      out->L = L;
+      out->mu = mu;
+      out->lambda = lam;
+      out->q = q;
+      out->feat[5] = (float)(lam / L);
+      // UpdateAlpha (:103-113) and beta (:226): the sequence is consumed in FP32 by the
+      // solver, so it is generated in FP32 (a serial FP64 chain would dominate the kernel)
+      float alpha = 1.0f;
+      const float qf = (float)q;
+      for (int it = 0; it < kMaxInner; ++it) {
+        const float b = alpha * alpha - qf, c = -alpha * alpha;
+        const float na = (-b + sqrtf(b * b - 4.0f * c)) * 0.5f;
+        out->beta[it] = alpha * (1.0f - alpha) / (alpha * alpha + na);
+        alpha = na;
+      }
+      out->status = (isfinite(L) && isfinite(mu)) ? 0 : PTG_ERR_NUMERIC;
+      s_scalar[0] = L;
     }
-    // GLambda, include/NesterovMNLS.hpp:75-91
-    double q = mu / L, lam;
-    if (1.0 / q > 1e6) lam = 10.0 * mu;
-    else if (1.0 / q > 1e3) lam = mu;
-    else lam = mu / 10.0;
-    L += lam;
-    mu += lam;
-    q = mu / L;
-    out->L = L;
-    out->mu = mu;
-    out->lambda = lam;
-    out->q = q;
-    out->feat[5] = (float)(lam / L);
-    // UpdateAlpha (:103-113) and beta (:226): the sequence is consumed in FP32 by the
-    // solver, so it is generated in FP32 (a serial FP64 chain would dominate the kernel)
-    float alpha = 1.0f;
-    const float qf = (float)q;
-    for (int it = 0; it < kMaxInner; ++it) {
-      const float b = alpha * alpha - qf, c = -alpha * alpha;
-      const float na = (-b + sqrtf(b * b - 4.0f * c)) * 0.5f;
-      out->beta[it] = alpha * (1.0f - alpha) / (alpha * alpha + na);
-      alpha = na;
-    }
-    out->status = (isfinite(L) && isfinite(mu)) ? 0 : PTG_ERR_NUMERIC;
-    s_scalar[0] = L;
   }
 }
 
