@@ -33,6 +33,7 @@ struct AlsBuffers {
   float *TD = nullptr;                  // the deeper node tensors (orders >= 5)
   float *gpart = nullptr;
   NnlsParams *np = nullptr;
+  NnlsParams *np_acc = nullptr;   // mode 0's bounds for the line-search point, computed beside it
   double *dsc = nullptr;  // [N][2]: <M, A>, sum(Z .* G); [0][2..3]: cost terms of a point;
                           // [4N], [4N + 1]: the line-search decision (accel_select_kernel)
   int *isc = nullptr;     // [N][2]: iterations, repaired; [2N]: the line search's stop gate;
@@ -74,6 +75,7 @@ struct AlsBuffers {
     const size_t o_TD = take(sizeof(float) * std::max<size_t>(deep_floats, 1));
     const size_t o_gp = take(sizeof(float) * gp);
     const size_t o_np = take(sizeof(NnlsParams));
+    const size_t o_npa = take(sizeof(NnlsParams));
     const size_t o_d = take(sizeof(double) * (4 * N + 2));
     const size_t o_i = take(sizeof(int) * (2 * N + 2));
     const size_t o_W = take(sizeof(double) * R * R);
@@ -98,6 +100,7 @@ struct AlsBuffers {
     TD = (float *)(b + o_TD);
     gpart = (float *)(b + o_gp);
     np = (NnlsParams *)(b + o_np);
+    np_acc = (NnlsParams *)(b + o_npa);
     dsc = (double *)(b + o_d);
     isc = (int *)(b + o_i);
     W = (double *)(b + o_W);
@@ -130,6 +133,8 @@ struct SelectArgs {
   const float *gacc[PTG_MAX_ORDER];
   double *sel;           // out: [0] the point's f^2, [1] 1.0 when taken
   int *taken;            // out: 1 when taken, else 0
+  const NnlsParams *np_acc;   // mode 0's bounds from the point's Grams ...
+  NnlsParams *np;             // ... installed for the next sweep when the point is taken
 };
 
 __global__ void accel_select_kernel(const SelectArgs a) {
@@ -149,6 +154,12 @@ __global__ void accel_select_kernel(const SelectArgs a) {
   __syncthreads();
   if (!take) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  {
+    const int64_t nw = (int64_t)(sizeof(NnlsParams) / sizeof(double));
+    const double *src = reinterpret_cast<const double *>(a.np_acc);
+    double *dst = reinterpret_cast<double *>(a.np);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nw; i += stride) dst[i] = src[i];
+  }
   for (int k = 0; k < a.N; ++k) {
     const int64_t n = (int64_t)a.rows[k] * a.R;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride) a.fac[k][i] = a.acc[k][i];
@@ -200,7 +211,8 @@ struct Runner {
   // copied to pinned memory behind them (ctx->ev_cost); nothing waits.  reuse_m0: a device
   // word that, when nonzero, cancels mode 0's MTTKRP because M already holds it (the line
   // search before this sweep took its point, whose cost it computed from that product).
-  int sweep_enqueue(const ptg_tensor *X, const int *reuse_m0 = nullptr) {
+  // np0_ready: mode 0's bounds are already in b.np (computed beside the line search).
+  int sweep_enqueue(const ptg_tensor *X, const int *reuse_m0 = nullptr, bool np0_ready = false) {
     cudaStream_t S = ctx->stream, T = ctx->side;
     const int N = b.N, R = b.R;
     if (dimtree) tree.new_sweep();   // normalisation and the line search changed every factor
@@ -210,13 +222,16 @@ struct Runner {
         PTG_TRY(other_update(X, n));
         continue;
       }
-      PTG_CUDA(cudaEventRecord(ctx->ev_fork, S));
-      PTG_CUDA(cudaStreamWaitEvent(T, ctx->ev_fork, 0));
-      // beside the tensor-core MTTKRP: a direct contraction, or the node contraction of a tree
-      const bool beside_tc = contraction_uses_tc(ctx, X, R) && (!dimtree || n == 0 || n == dimtree_split(N));
-      PTG_TRY(launch_eigen_bounds(b.gram, N, n, R, b.np, T, beside_tc));
-      count_launches(ctx, 1);
-      PTG_CUDA(cudaEventRecord(ctx->ev_join, T));
+      const bool bounds = !(n == 0 && np0_ready);
+      if (bounds) {
+        PTG_CUDA(cudaEventRecord(ctx->ev_fork, S));
+        PTG_CUDA(cudaStreamWaitEvent(T, ctx->ev_fork, 0));
+        // beside the tensor-core MTTKRP: a direct contraction, or the node contraction of a tree
+        const bool beside_tc = contraction_uses_tc(ctx, X, R) && (!dimtree || n == 0 || n == dimtree_split(N));
+        PTG_TRY(launch_eigen_bounds(b.gram, N, n, R, b.np, T, beside_tc));
+        count_launches(ctx, 1);
+        PTG_CUDA(cudaEventRecord(ctx->ev_join, T));
+      }
       if (!dimtree) {
         Contraction c = mttkrp_contraction(X, b.fac, n);
         if (n == 0) c.skip = reuse_m0;
@@ -226,7 +241,7 @@ struct Runner {
         // are recomputed (the root's children once per sweep, before modes 0 and h)
         PTG_TRY(tree.mttkrp(ctx, X, b.fac, n, R, b.M, S));
       }
-      PTG_CUDA(cudaStreamWaitEvent(S, ctx->ev_join, 0));
+      if (bounds) PTG_CUDA(cudaStreamWaitEvent(S, ctx->ev_join, 0));
       PTG_TRY(launch_nnls_full(ctx, b.M, b.fac[n], b.rows[n], R, b.np, (float)opt->nesterov_delta_1,
                                (float)opt->nesterov_delta_2, b.gram[n], b.dsc + 4 * n,
                                b.dsc + 4 * n + 1, b.isc + 2 * n, b.isc + 2 * n + 1, S, warm[n]));
@@ -295,6 +310,8 @@ struct Runner {
     }
     a.sel = b.dsc + 4 * b.N;
     a.taken = b.isc + 2 * b.N + 1;
+    a.np_acc = b.np_acc;
+    a.np = b.np;
     const int blocks = (int)std::min<int64_t>((most + 255) / 256, (int64_t)ctx->sm_count);
     accel_select_kernel<<<std::max(blocks, 1), 256, 0, S>>>(a);
     PTG_CUDA(cudaGetLastError());
@@ -538,7 +555,8 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
     // line search took its point, its mode-0 MTTKRP is this sweep's first one (direct
     // contractions; a tree's nodes would be stale).
     const bool m0_reusable = sel_pending && !run.dimtree && opt.constraints[0] == PTG_NONNEGATIVITY;
-    PTG_TRY(run.sweep_enqueue(Xa, m0_reusable ? b.isc + 2 * N + 1 : nullptr));
+    const bool np0_ready = sel_pending && opt.constraints[0] == PTG_NONNEGATIVITY;
+    PTG_TRY(run.sweep_enqueue(Xa, m0_reusable ? b.isc + 2 * N + 1 : nullptr, np0_ready));
     if (model && ao_iter == log_sweeps && opt.warm_train_steps > 0) {
       double loss = 0.0;
       PTG_TRY(ptg_mlp_train(ctx, model, logX, logT, logged, opt.warm_train_steps, 256, 1e-3f, 1234, &loss));
@@ -568,13 +586,31 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
         for (int k = 0; k < N; ++k)
           PTG_CUDA(cudaMemcpyAsync(b.old[k], b.fac[k], sizeof(float) * b.rows[k] * rank,
                                    cudaMemcpyDeviceToDevice, T));
+        // the next sweep's mode-0 bounds for both outcomes, beside the point's MTTKRP: from the
+        // point's Grams (installed by accel_select_kernel if it is taken) and from the current
+        // ones (the sweep's own, normalised); that sweep then launches none for mode 0
+        // (ev_join: the point's Grams, for its cost terms; ev_join2/3: the two bounds, for
+        // accel_select_kernel, which may install one over the other)
         PTG_CUDA(cudaEventRecord(ctx->ev_join, T));
+        const bool np0 = opt.constraints[0] == PTG_NONNEGATIVITY;
+        if (np0) {
+          PTG_TRY(launch_eigen_bounds(b.gacc, N, 0, rank, b.np_acc, T, beside_tc));
+          PTG_CUDA(cudaEventRecord(ctx->ev_join3, T));
+          PTG_CUDA(cudaStreamWaitEvent(ctx->side2, ctx->ev_fork, 0));
+          PTG_TRY(launch_eigen_bounds(b.gram, N, 0, rank, b.np, ctx->side2, beside_tc));
+          PTG_CUDA(cudaEventRecord(ctx->ev_join2, ctx->side2));
+          count_launches(ctx, 2);
+        }
         count_launches(ctx, 1 + 2 * N);
         int *gate = b.isc + 2 * N;
         stop_gate_kernel<<<1, 1, 0, S>>>(b.dsc, N - 1, frob, opt.threshold_error, ao_iter, opt.max_iter, gate);
         PTG_CUDA(cudaGetLastError());
         count_launches(ctx, 1);
         PTG_TRY(run.point_cost_enqueue(Xa, b.acc, b.gacc, gate, ctx->ev_join));
+        if (np0) {
+          PTG_CUDA(cudaStreamWaitEvent(S, ctx->ev_join3, 0));
+          PTG_CUDA(cudaStreamWaitEvent(S, ctx->ev_join2, 0));
+        }
         PTG_TRY(run.select_enqueue(frob, opt.threshold_error, ao_iter, opt.max_iter));
         sel_pending = true;
         sel_sweep = ntrace;

@@ -260,8 +260,11 @@ int ptg_ctx_create(int device, ptg_ctx **out) {
   c->pageable_ats = pageable == 1 && host_tables == 1;
   cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join3, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_cost, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_sel, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaHostAlloc(&c->pinned_scalars, kPinnedScalarBytes, cudaHostAllocDefault);
@@ -291,10 +294,13 @@ int ptg_ctx_destroy(ptg_ctx *c) {
   c->cache_xr.release();
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->ev_join2) cudaEventDestroy(c->ev_join2);
+  if (c->ev_join3) cudaEventDestroy(c->ev_join3);
   if (c->ev_cost) cudaEventDestroy(c->ev_cost);
   if (c->ev_sel) cudaEventDestroy(c->ev_sel);
   if (c->pinned_scalars) cudaFreeHost(c->pinned_scalars);
   if (c->side) cudaStreamDestroy(c->side);
+  if (c->side2) cudaStreamDestroy(c->side2);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return PTG_OK;

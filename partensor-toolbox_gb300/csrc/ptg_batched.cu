@@ -163,18 +163,22 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   return t;
 }
 
+// The items of one MTTKRP on the CTA's 128-thread groups g0..kPGroups-1 (the calling
+// thread's group is threadIdx.x / 128; groups below g0 are busy with other work).
 template <int BN, bool MM, int BM>
-__device__ void cta_mttkrp_cfg(const SimtParams &prm, int nsplit, float *sm, int group_floats) {
-  const int g = threadIdx.x >> 7, gt = threadIdx.x & 127;
+__device__ void cta_mttkrp_cfg(const SimtParams &prm, int nsplit, float *sm, int group_floats, int g0) {
+  const int g = (threadIdx.x >> 7) - g0, gt = threadIdx.x & 127, ng = kPGroups - g0;
   const int mtiles = (int)((prm.Q + BM - 1) / BM);
   const int items = mtiles * nsplit;
   float *gs = sm + (size_t)g * group_floats;
-  for (int it = g; it < items; it += kPGroups)
-    mttkrp_simt_body<float, BN, MM, BM, SyncGroup128>(prm, it / nsplit, it % nsplit, gs, gt, SyncGroup128{1 + g});
+  for (int it = g; it < items; it += ng)
+    mttkrp_simt_body<float, BN, MM, BM, SyncGroup128>(prm, it / nsplit, it % nsplit, gs, gt,
+                                                      SyncGroup128{1 + g0 + g});
 }
 
-// MTTKRP of contraction `set` of instance i into its M buffer (every thread of the CTA).
-__device__ void cta_mttkrp(const PersistArgs &a, int i, int set, float *sm, float *scr, SimtParams *s_prm) {
+// MTTKRP of contraction `set` of instance i into its M buffer, in three steps: the setup and
+// the split sum are CTA-wide (every thread calls them); the items run on groups g0.. only.
+__device__ PMeta cta_mttkrp_setup(const PersistArgs &a, int i, int set, float *scr, SimtParams *s_prm) {
   const int k = i * (a.N + 1) + set;
   const PMeta m = a.meta[k];
   if (threadIdx.x == 0) {
@@ -183,24 +187,30 @@ __device__ void cta_mttkrp(const PersistArgs &a, int i, int set, float *sm, floa
     s_prm->nsplit = m.nsplit;
   }
   __syncthreads();
-  const SimtParams &p = *s_prm;
+  return m;
+}
+
+__device__ void cta_mttkrp_items(const PMeta &m, const SimtParams &p, float *sm, int group_floats, int g0) {
   if (m.bn == 16) {
     if (m.mmajor) {
-      if (m.bm == 64) cta_mttkrp_cfg<16, true, 64>(p, m.nsplit, sm, a.group_floats);
-      else cta_mttkrp_cfg<16, true, 128>(p, m.nsplit, sm, a.group_floats);
+      if (m.bm == 64) cta_mttkrp_cfg<16, true, 64>(p, m.nsplit, sm, group_floats, g0);
+      else cta_mttkrp_cfg<16, true, 128>(p, m.nsplit, sm, group_floats, g0);
     } else {
-      if (m.bm == 64) cta_mttkrp_cfg<16, false, 64>(p, m.nsplit, sm, a.group_floats);
-      else cta_mttkrp_cfg<16, false, 128>(p, m.nsplit, sm, a.group_floats);
+      if (m.bm == 64) cta_mttkrp_cfg<16, false, 64>(p, m.nsplit, sm, group_floats, g0);
+      else cta_mttkrp_cfg<16, false, 128>(p, m.nsplit, sm, group_floats, g0);
     }
   } else {
     if (m.mmajor) {
-      if (m.bm == 64) cta_mttkrp_cfg<32, true, 64>(p, m.nsplit, sm, a.group_floats);
-      else cta_mttkrp_cfg<32, true, 128>(p, m.nsplit, sm, a.group_floats);
+      if (m.bm == 64) cta_mttkrp_cfg<32, true, 64>(p, m.nsplit, sm, group_floats, g0);
+      else cta_mttkrp_cfg<32, true, 128>(p, m.nsplit, sm, group_floats, g0);
     } else {
-      if (m.bm == 64) cta_mttkrp_cfg<32, false, 64>(p, m.nsplit, sm, a.group_floats);
-      else cta_mttkrp_cfg<32, false, 128>(p, m.nsplit, sm, a.group_floats);
+      if (m.bm == 64) cta_mttkrp_cfg<32, false, 64>(p, m.nsplit, sm, group_floats, g0);
+      else cta_mttkrp_cfg<32, false, 128>(p, m.nsplit, sm, group_floats, g0);
     }
   }
+}
+
+__device__ void cta_mttkrp_finish(const PMeta &m, const SimtParams &p, const float *scr) {
   __syncthreads();
   if (m.nsplit > 1) {   // the partials of every split, summed in split order
     const int R = p.R, bn = m.bn;
@@ -212,6 +222,12 @@ __device__ void cta_mttkrp(const PersistArgs &a, int i, int set, float *sm, floa
     }
     __syncthreads();
   }
+}
+
+__device__ void cta_mttkrp(const PersistArgs &a, int i, int set, float *sm, float *scr, SimtParams *s_prm) {
+  const PMeta m = cta_mttkrp_setup(a, i, set, scr, s_prm);
+  cta_mttkrp_items(m, *s_prm, sm, a.group_floats, 0);
+  cta_mttkrp_finish(m, *s_prm, scr);
 }
 
 // The ALS loop of one instance (include/Cpd.hpp:288-356 with the batched path's per-instance
@@ -240,9 +256,17 @@ __device__ void persist_instance(const PersistArgs &a, int i, float *sm, float *
       const EigDesc &e = a.eig[(size_t)n * a.n_inst + i];
       GramPtrs gp{};
       for (int k = 0; k < N; ++k) gp.g[k] = e.gram[k];
-      eigen_bounds_body<BN_THREADS>(gp, N, n, e.R, e.out);
-      __syncthreads();
-      if (n != 0 || !reuse_m0) cta_mttkrp(a, i, n, sm, scr, s_prm);
+      if (n == 0 && reuse_m0) {   // M already holds mode 0's MTTKRP: the bounds alone
+        if (threadIdx.x < 128) eigen_bounds_body<128, SyncGroup128>(gp, N, n, e.R, e.out, threadIdx.x, SyncGroup128{5});
+        __syncthreads();
+      } else {
+        // the FP64 bounds on warps 0-3 (their own barrier) beside the MTTKRP's items on the
+        // other three groups: the bounds mostly wait on the FP64 pipe, the MTTKRP on the FP32 one
+        const PMeta m = cta_mttkrp_setup(a, i, n, scr, s_prm);
+        if (threadIdx.x < 128) eigen_bounds_body<128, SyncGroup128>(gp, N, n, e.R, e.out, threadIdx.x, SyncGroup128{5});
+        else cta_mttkrp_items(m, *s_prm, sm, a.group_floats, 1);
+        cta_mttkrp_finish(m, *s_prm, scr);
+      }
       nnls_block_body(a.nn[(size_t)n * a.n_inst + i], sm);
       __syncthreads();
     }

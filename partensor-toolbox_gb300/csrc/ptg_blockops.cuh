@@ -6,6 +6,7 @@
 #include <cmath>
 
 #include "ptg_internal.h"
+#include "ptg_sync.cuh"
 
 namespace ptg {
 namespace {
@@ -71,9 +72,12 @@ __device__ int sturm_count_f64s(const double *d, const double *e2, int n, double
   return cnt;
 }
 
-// NT threads (a multiple of 64, at least 128) take part; every one of them must call it.
-template <int NT = kEigThreads>
-__device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R, NnlsParams *out) {
+// NT threads (a multiple of 64, at least 128) take part, with indices tid in [0, NT) and the
+// barrier `sync` among them (the whole CTA, or a 128-thread group beside other work); every
+// one of them must call it.
+template <int NT = kEigThreads, typename Sync = SyncCta>
+__device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R, NnlsParams *out, int tid,
+                                  Sync sync = Sync()) {
   static_assert(NT % kMaxR == 0 && NT >= 128, "eigenvalue-bound thread count");
   constexpr int lda = kMaxR + 1;              // padded rows: column reads and mirrored writes
   __shared__ double A[kMaxR * lda];           // spread over the banks
@@ -84,12 +88,11 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
   __shared__ double s_scalar[4];
   __shared__ double lohi[2][2];
   __shared__ float df[kMaxR], e2f[kMaxR];
-  const int tid = threadIdx.x;
   const int n = R;
 
   // Z = prod_{k != mode} G_k (FP64), k from order-1 down to 0 as PartialCwiseProd orders it;
   // the tridiagonalisation works on the lower triangle mirrored, so A is exactly symmetric
-  for (int idx = tid; idx < n * n; idx += blockDim.x) {
+  for (int idx = tid; idx < n * n; idx += NT) {
     const int i = idx / n, j = idx - (idx / n) * n;
     double z = 1.0;
     for (int k = order - 1; k >= 0; --k)
@@ -100,7 +103,7 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
       A[j * lda + i] = z;
     }
   }
-  __syncthreads();
+  sync();
 
   // Block sum: warp shuffles, then every thread adds the warps' partials in warp order from one
   // of two alternating buffers, so a sum costs one barrier and no broadcast.  (A buffer is
@@ -109,7 +112,7 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
   auto block_sum = [&](double x) -> double {
     for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
     if ((tid & 31) == 0) redb[rb][tid >> 5] = x;
-    __syncthreads();
+    sync();
     // every warp sums the partials by a butterfly: the same bits in every lane (each step
     // adds the same two values), five FP64 additions instead of one per warp
     double v = (tid & 31) < NT / 32 ? redb[rb][tid & 31] : 0.0;
@@ -153,7 +156,7 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
       s_scalar[0] = al;
       s_scalar[3] = 2.0 / (dv * dv + sigma);
     }
-    __syncthreads();
+    sync();
     const double alpha = s_scalar[0], beta = s_scalar[3];
     const double v0 = x0 - alpha;
     double pv = 0.0, vi = 0.0, pvi = 0.0;
@@ -169,8 +172,8 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
       vs[tid] = vi;
       ws[tid] = pvi - K * vi;
     }
-    __syncthreads();
-    for (int idx = tid; idx < m * m; idx += blockDim.x) {
+    sync();
+    for (int idx = tid; idx < m * m; idx += NT) {
       const int i = idx / m, j = idx - (idx / m) * m;
       if (j > i) continue;
       const double a = A[(k + 1 + i) * lda + (k + 1 + j)] - (vs[i] * ws[j] + ws[i] * vs[j]);
@@ -178,14 +181,14 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
       A[(k + 1 + j) * lda + (k + 1 + i)] = a;
     }
     if (tid == 0) e[k] = alpha;
-    __syncthreads();
+    sync();
   }
   // ---- T = (d, e) scaled by a power of two, sc, so that its Gershgorin interval lies in
   // [-1, 1]; the counts and the bisection run on the scaled T (exact), the result is scaled
   // back at the end ----
   for (int i = tid; i < n; i += NT) d[i] = A[i * lda + i];
   if (tid == 0 && n >= 2) e[n - 2] = A[(n - 1) * lda + (n - 2)];
-  __syncthreads();
+  sync();
   if (tid < 32) {   // warp 0: the Gershgorin interval
     double glo = 1e300, ghi = -1e300;
     for (int i = tid; i < n; i += 32) {
@@ -210,7 +213,7 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
       s_scalar[2] = sc;
     }
   }
-  __syncthreads();
+  sync();
   {
     const double sc = s_scalar[2];
     for (int i = tid; i < n; i += NT) {
@@ -224,7 +227,7 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
       }
     }
   }
-  __syncthreads();   // d and e2 are complete before any thread reads them (n > 32 spans warps)
+  sync();   // d and e2 are complete before any thread reads them (n > 32 spans warps)
 
   // ---- bisection: warp 0 brackets the smallest eigenvalue, warp 1 the largest, with a
   // 32-way multisection per round: FP32 counts first, then FP64 counts on the widened
@@ -280,7 +283,7 @@ __device__ void eigen_bounds_body(const GramPtrs &gp, int order, int mode, int R
       lohi[which][1] = hi;
     }
   }
-  __syncthreads();
+  sync();
   if (tid < 32) {
     // scale-free summaries of Z for the warm-start network: its diagonal's sum, min and max
     double dsum = 0.0, dmin = 1e300, dmax = -1e300;

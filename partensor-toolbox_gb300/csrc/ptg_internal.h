@@ -67,7 +67,8 @@ struct ptg_ctx {
   cudaStream_t stream = nullptr;      // main stream (own or caller's)
   cudaStream_t own_stream = nullptr;
   cudaStream_t side = nullptr;        // concurrent small kernels (FP64 eigenbounds)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaStream_t side2 = nullptr;       // a second one (the line search's speculative bounds)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr, ev_join3 = nullptr;
   ptg::DevBuf scratch;                // split-K partials and other temporaries
   int nnls_cluster = 0;               // cluster size the NNLS kernel launched with (0 = unknown)
   ptg_ctx_stats stats;

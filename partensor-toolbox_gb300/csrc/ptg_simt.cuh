@@ -5,6 +5,7 @@
 #include <cuda_bf16.h>
 
 #include "ptg_internal.h"
+#include "ptg_sync.cuh"
 
 namespace ptg {
 namespace {
@@ -75,16 +76,6 @@ __device__ __forceinline__ void kr_side(const KrDev &s, uint32_t lin, int R, int
     for (int j = 0; j < NV; ++j) v[j] *= (c + j < R) ? __ldg(row + c + j) : 0.0f;
   }
 }
-
-// The barrier a tile routine uses: the whole CTA, or one 128-thread group of a larger CTA
-// (named barrier `id`, so that several groups work on different tiles independently).
-struct SyncCta {
-  __device__ __forceinline__ void operator()() const { __syncthreads(); }
-};
-struct SyncGroup128 {
-  int id;   // 1..15 (0 is __syncthreads' barrier)
-  __device__ __forceinline__ void operator()() const { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
-};
 
 // Tile configuration: BN columns per launch, BM rows of Q, BK contraction elements.
 template <int BN>

@@ -29,7 +29,7 @@ namespace {
 
 __global__ void __launch_bounds__(kEigThreads)
 eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
-  eigen_bounds_body<kEigThreads>(gp, order, mode, R, out);
+  eigen_bounds_body<kEigThreads>(gp, order, mode, R, out, threadIdx.x);
 }
 
 // ------------------------------------------------------------------------------------
@@ -796,7 +796,7 @@ __global__ void __launch_bounds__(kEigThreads) eigen_batched_kernel(const EigDes
   if (active && !active[e.inst]) return;
   GramPtrs gp{};
   for (int k = 0; k < e.order; ++k) gp.g[k] = e.gram[k];
-  eigen_bounds_body<kEigThreads>(gp, e.order, e.mode, e.R, e.out);
+  eigen_bounds_body<kEigThreads>(gp, e.order, e.mode, e.R, e.out, threadIdx.x);
 }
 
 __global__ void gram_batched_kernel(const InstDesc *__restrict__ d, const int *__restrict__ active, int use_acc) {
