@@ -37,6 +37,7 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
 // ------------------------------------------------------------------------------------
 constexpr int kNnlsWarps = 16;
 constexpr int kNnlsThreads = kNnlsWarps * 32;
+constexpr int kNnlsWindowMax = 8;
 
 struct NnlsArgs {
   const float *M;        // [I][R]
@@ -54,6 +55,7 @@ struct NnlsArgs {
   int hidden;
   float *log_X;          // [I][R + 8] features of each row (optional)
   float *log_T;          // [I][R] solution scaled by L / ||m_i|| (optional)
+  int window;            // iterations per cluster barrier, 1..kNnlsWindowMax (launch sets it)
 };
 
 template <int RB, int ROWS>
@@ -66,15 +68,17 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
 
   extern __shared__ __align__(16) float sm[];
   float *Zt = sm;                                   // R*R
-  float *As = Zt + R * R;                           // (kNnlsWarps*ROWS) x R
-  float *Gp = As + kNnlsWarps * ROWS * R;           // R*R  (this CTA's partial Gram)
+  const int KW = a.window;
+  float *As = Zt + R * R;                           // KW slots of (kNnlsWarps*ROWS) x R: A_it per step
+  const int aslot = kNnlsWarps * ROWS * R;
+  float *Gp = As + KW * aslot;                      // R*R  (this CTA's partial Gram)
   float *colsum = Gp + R * R;                       // R
   float *slots = colsum + ((R + 1) & ~1);          // [2][2] stop test (max |g.y|, min g)
   float *wred = slots + 4;                          // kNnlsWarps * 2
   double *wredd = reinterpret_cast<double *>(wred + 2 * kNnlsWarps);   // kNnlsWarps
   double *ma = wredd + kNnlsWarps;                  // 1: this CTA's <M, A>
-  int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired, [1..3]: stop-test words, [4..7]: unused
-  float *bt = reinterpret_cast<float *>(flags + 8); // kMaxInner: the beta sequence
+  int *flags = reinterpret_cast<int *>(ma + 2);     // [0]: repaired, [8..32): stop-test words
+  float *bt = reinterpret_cast<float *>(flags + 8 + 3 * kNnlsWindowMax);   // kMaxInner: the beta sequence
   float *rsc = bt + kMaxInner;                      // kNnlsWarps*ROWS: row scales of the warm start
   // RB == 1 only: the warps' Y rows, (kNnlsWarps*ROWS) x 32, on a 16-byte boundary
   float *Ys = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(rsc + kNnlsWarps * ROWS) + 15) &
@@ -235,14 +239,16 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
 
   // Global stop test without a reduction: the test of include/NesterovMNLS.hpp:217-218
   // (max |grad .* Y| <= delta1 and min grad >= -delta2) fails iff some element violates it,
-  // so each warp that sees a violation writes 1 into a flag word of iteration `it` in CTA 0's
-  // shared memory (three words used in rotation).  One split cluster barrier per iteration:
-  // arrive after the flag write and the speculative update, wait after the next gradient, so
-  // the barrier's latency hides behind that product.  The update of iteration `it` keeps A_it
-  // in the staging rows (As) in case the flag says stop.  (Copies of the words in every CTA,
-  // written by lanes 0..CS-1 of a violating warp and read locally, measured no faster.)
-  int *vflag0 = cluster.map_shared_rank(flags + 1, 0);
-  if (tid < 3) flags[1 + tid] = 0;
+  // so each warp that sees a violation at an iteration writes 1 into that iteration's flag
+  // word in CTA 0's shared memory.  Rows are independent apart from this test, so the
+  // iterations run in windows of KW steps with one split cluster barrier per window: every
+  // step keeps its A_it in a slot of As, and after the barrier the first step of the window
+  // whose word is still 0 is where the reference stops (its A_it is the result); the steps
+  // after it were speculative.  The barrier is split: arrive after the window's last update,
+  // wait after the next gradient, so its latency hides behind that product.  The words of
+  // three windows are used in rotation.
+  int *vflag0 = cluster.map_shared_rank(flags + 8, 0);
+  if (tid < 3 * kNnlsWindowMax) flags[8 + tid] = 0;
   cluster.sync();
   float g[ROWS][RB];
   // R <= 32: this lane's column of Z~ stays in registers for the whole solve and the warp's
@@ -296,41 +302,55 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   stage_y();
   gradient();
   int it = 0;
-  for (;;) {
-    if (it >= kMaxInner) break;   // A_it is the result
-    bool viol = false;
+  for (int w = 0; it < kMaxInner; ++w) {
+    const int wslot = (w % 3) * kNnlsWindowMax;
+    const int t0 = it;
+    int steps = 0;
+    for (; steps < KW && it < kMaxInner; ++steps, ++it) {
+      bool viol = false;
 #pragma unroll
-    for (int j = 0; j < ROWS; ++j) {
-      const bool rowok = (gw + j * stride) < I;
+      for (int j = 0; j < ROWS; ++j) {
+        const bool rowok = (gw + j * stride) < I;
 #pragma unroll
-      for (int b = 0; b < RB; ++b)
-        if (rowok && colok[b]) viol |= (fabsf(g[j][b] * Y[j][b]) > a.delta1) || (g[j][b] < -a.delta2);
-    }
-    if (__any_sync(0xffffffffu, viol) && lane == 0) *(volatile int *)&vflag0[it % 3] = 1;
-    if (rank == 0 && tid == 0) flags[1 + (it + 1) % 3] = 0;   // the word of it+1 (read last at it-2)
-    const float beta = bt[it];
-#pragma unroll
-    for (int j = 0; j < ROWS; ++j)
-#pragma unroll
-      for (int b = 0; b < RB; ++b) {
-        if (colok[b]) As[(warp * ROWS + j) * R + lane + 32 * b] = Ac[j][b];   // A_it
-        const float na = fmaxf(Y[j][b] - g[j][b] * invL, 0.0f);       // :220
-        Y[j][b] = (1.0f + beta) * na - beta * Ac[j][b];                 // :228
-        Ac[j][b] = na;
+        for (int b = 0; b < RB; ++b)
+          if (rowok && colok[b]) viol |= (fabsf(g[j][b] * Y[j][b]) > a.delta1) || (g[j][b] < -a.delta2);
       }
+      if (__any_sync(0xffffffffu, viol) && lane == 0) *(volatile int *)&vflag0[wslot + steps] = 1;
+      const float beta = bt[it];
+      float *slot = As + steps * aslot;
+#pragma unroll
+      for (int j = 0; j < ROWS; ++j)
+#pragma unroll
+        for (int b = 0; b < RB; ++b) {
+          if (colok[b]) slot[(warp * ROWS + j) * R + lane + 32 * b] = Ac[j][b];   // A_it
+          const float na = fmaxf(Y[j][b] - g[j][b] * invL, 0.0f);       // :220
+          Y[j][b] = (1.0f + beta) * na - beta * Ac[j][b];                 // :228
+          Ac[j][b] = na;
+        }
+      if (steps + 1 < KW && it + 1 < kMaxInner) {   // the next step of this window
+        stage_y();
+        gradient();
+      }
+    }
+    // the words of window w+1 (read last in window w-2, before every CTA's arrive of w-1)
+    if (rank == 0 && tid < kNnlsWindowMax) flags[8 + ((w + 1) % 3) * kNnlsWindowMax + tid] = 0;
     asm volatile("barrier.cluster.arrive.release;" ::: "memory");
     stage_y();
-    gradient();   // of it+1 (discarded if it stops at it)
+    gradient();   // of the next window's first step (discarded if the solve stops here)
     asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
-    if (*(volatile int *)&vflag0[it % 3] == 0) {   // no violation: stop, the result is A_it
+    const int wv = lane < steps ? *(volatile int *)&vflag0[wslot + lane] : 1;
+    const unsigned clear = __ballot_sync(0xffffffffu, wv == 0);
+    if (clear) {   // the first step without a violation: stop there, the result is its A_it
+      const int first = __ffs(clear) - 1;
+      it = t0 + first;
+      const float *slot = As + first * aslot;
 #pragma unroll
       for (int j = 0; j < ROWS; ++j)
 #pragma unroll
         for (int b = 0; b < RB; ++b)
-          if (colok[b]) Ac[j][b] = As[(warp * ROWS + j) * R + lane + 32 * b];
+          if (colok[b]) Ac[j][b] = slot[(warp * ROWS + j) * R + lane + 32 * b];
       break;
     }
-    ++it;
   }
 
   // ---- zero-column test (sum of |A| per column over all rows), include/Cpd.hpp:206 ----
@@ -438,16 +458,20 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
 }
 
 template <int RB, int ROWS>
-size_t nnls_smem_bytes(int R) {
-  return sizeof(float) * (2 * R * R + kNnlsWarps * ROWS * R + ((R + 1) & ~1) + 4 + 2 * kNnlsWarps) +
-         sizeof(double) * (kNnlsWarps + 2) + 32 + sizeof(float) * (kMaxInner + kNnlsWarps * ROWS) +
-         (RB == 1 ? 16 + sizeof(float) * kNnlsWarps * ROWS * 32 : 0);
+size_t nnls_smem_bytes(int R, int window) {
+  return sizeof(float) * (2 * R * R + (size_t)window * kNnlsWarps * ROWS * R + ((R + 1) & ~1) + 4 + 2 * kNnlsWarps) +
+         sizeof(double) * (kNnlsWarps + 2) + sizeof(int) * (8 + 3 * kNnlsWindowMax) +
+         sizeof(float) * (kMaxInner + kNnlsWarps * ROWS) + (RB == 1 ? 16 + sizeof(float) * kNnlsWarps * ROWS * 32 : 0);
 }
 
 template <int RB, int ROWS>
-int launch_nnls_t(int cs, const NnlsArgs &args, cudaStream_t stream) {
+int launch_nnls_t(int cs, const NnlsArgs &args_in, cudaStream_t stream) {
   auto kern = nnls_cluster_kernel<RB, ROWS>;
-  const size_t smem = nnls_smem_bytes<RB, ROWS>(args.R);
+  // as many iterations per cluster barrier as the A_it slots fit in 96 KB (at most 8)
+  NnlsArgs args = args_in;
+  const size_t slot = sizeof(float) * kNnlsWarps * ROWS * args.R;
+  args.window = (int)std::max<size_t>(1, std::min<size_t>(kNnlsWindowMax, (96u << 10) / slot));
+  const size_t smem = nnls_smem_bytes<RB, ROWS>(args.R, args.window);
   PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (cs > 8) PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   if ((int64_t)cs * kNnlsWarps * ROWS < args.I)
@@ -474,7 +498,7 @@ int nnls_cluster_size(ptg_ctx *ctx) {
   if (ctx->nnls_cluster) return ctx->nnls_cluster;
   int cs = 8;
   auto kern = nnls_cluster_kernel<2, 16>;
-  const size_t smem = nnls_smem_bytes<2, 16>(kMaxR);
+  const size_t smem = nnls_smem_bytes<2, 16>(kMaxR, 1);   // the largest slot: one step per window
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess &&
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
