@@ -76,11 +76,11 @@ int ptg_ctx_synchronize(ptg_ctx *ctx);
 
 /* Context options (GB300 knobs, no reference counterpart). */
 typedef enum {
-  PTG_OPT_MTTKRP_IMPL = 1 /* 0: auto (tensor cores for BF16 and FP8 storage, CUDA cores for
-                             FP32), 1: CUDA cores (BF16, FP32), 2: tensor cores (BF16: kind::f16;
-                             FP32, R <= 64: kind::tf32 with a three-term split; each CTA's
-                             accumulation chain is capped at 2048 terms, and the accumulation
-                             still drifts low: -1.9e-5 relative at 10^6-term contractions) */,
+  PTG_OPT_MTTKRP_IMPL = 1 /* 0: auto (tensor cores for BF16, FP8 and, at R <= 64, FP32 storage),
+                             1: CUDA cores (BF16, FP32), 2: tensor cores (BF16: kind::f16; FP32,
+                             R <= 64: kind::tf32 with a three-term split, each accumulator
+                             drained into FP32 registers every 64 terms: -4e-7 relative bias at
+                             10^6-term contractions) */,
   PTG_OPT_NNLS_CLUSTER = 2 /* CTAs of the NNLS thread-block cluster: 0 auto (16 where the device
                              schedules it, else 8), or 2, 4, 8, 16 */,
   PTG_OPT_GTC_ROWS = 3 /* sparse row solver of the nonnegative GTC modes: 0 auto (one warp per

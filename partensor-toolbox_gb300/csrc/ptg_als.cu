@@ -274,10 +274,11 @@ struct Runner {
   // form (include/Cpd.hpp:262-266).  Mode 0 because, when the point is taken, that product
   // (left in b.M) is the next sweep's first MTTKRP, which the sweep then skips.
   int point_cost_enqueue(const ptg_tensor *X, float *const *factors, float *const *grams,
-                         const int *skip = nullptr, cudaEvent_t grams_ready = nullptr) {
+                         const int *skip = nullptr, cudaEvent_t grams_ready = nullptr, bool exact = false) {
     cudaStream_t S = ctx->stream;
     Contraction c = mttkrp_contraction(X, factors, 0);
     c.skip = skip;
+    c.exact_fp32 = exact;
     PTG_TRY(contraction_launch(ctx, X, c, b.R, b.M, S));
     if (grams_ready) PTG_CUDA(cudaStreamWaitEvent(S, grams_ready, 0));
     PTG_TRY(launch_cost_terms(b.M, factors[0], b.rows[0], grams, b.N, b.R, b.dsc + 2,
@@ -361,9 +362,9 @@ struct Runner {
 
   // cost of the point (factors, grams) by one MTTKRP: sqrt(||X||^2 + sum(Z.*G) - 2<M,A>)
   int point_cost(const ptg_tensor *X, double frob, float *const *factors, float *const *grams,
-                 double *f_out) {
+                 double *f_out, bool exact = false) {
     cudaStream_t S = ctx->stream;
-    PTG_TRY(point_cost_enqueue(X, factors, grams));
+    PTG_TRY(point_cost_enqueue(X, factors, grams, nullptr, nullptr, exact));
     double h[2];
     PTG_CUDA(cudaMemcpyAsync(h, b.dsc + 2, sizeof(h), cudaMemcpyDeviceToHost, S));
     PTG_TRY(check_device_error(ctx));
@@ -662,11 +663,12 @@ static int cpd_als_impl(ptg_ctx *ctx, const ptg_tensor *X, const ptg_tensor *ref
       ++ntrace;
     }
   }
-  // the cost of the final factors on the FP32 copy (one MTTKRP in the Gram form)
+  // the cost of the final factors on the FP32 copy (one MTTKRP in the Gram form, on the CUDA
+  // cores: unbiased)
   if (refine && refined == 0 && opt.verify_fp32) {
     Xa = refine;
     frob = cost_norm(Xa);
-    PTG_TRY(run.point_cost(Xa, frob, b.fac, b.gram, &f));
+    PTG_TRY(run.point_cost(Xa, frob, b.fac, b.gram, &f, true));
     rel = f / std::sqrt(frob);
   }
   // results: device FP32 row-major -> host FP64 ColMajor

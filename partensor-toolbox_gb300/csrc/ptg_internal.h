@@ -151,6 +151,10 @@ struct Contraction {
   // q / slab_div when slab_in_q (0: not set)
   int64_t slab_div = 0;
   bool slab_in_q = false;
+  // FP32 storage on the CUDA cores even where the TF32 tensor cores are the automatic choice:
+  // their accumulation keeps a ~4e-7 relative bias, which a fit's cancellation (f^2 = ||X||^2
+  // - 2<M, A> + ...) amplifies by ~1/rel^2; the fit that verify_fp32 reports has none
+  bool exact_fp32 = false;
 };
 
 // Whether the factor rows of a contraction can be read as float4: R % 4 == 0 and every

@@ -422,13 +422,12 @@ static double contraction_bytes(const ptg_tensor *t, const Contraction &c, int R
   return numel * esz + fac + (double)c.q_write * R * 4.0;
 }
 
-// FP32 storage reaches the tensor cores (three-term TF32 split) only on request: the FP32
-// accumulation in TMEM drifts low by ~2^-25 per accumulate step, so a chain of 512 steps (the
-// capped 64 K-blocks of a CTA) still carries a ~-1.9e-5 relative bias at 10^6-term
-// contractions, above the CUDA-core kernel's unbiased FP32 error.
+// FP32 storage reaches the tensor cores through the three-term TF32 split (R <= 64); its TMEM
+// accumulators are drained into FP32 registers every two K-blocks, which keeps the drift of
+// the tensor cores' accumulation (~2^-25 of the running sum per step) below 5e-7 relative.
 bool contraction_uses_tc(const ptg_ctx *ctx, const ptg_tensor *t, int R) {
   return t->dtype == PTG_FP8E4M3 || (t->dtype == PTG_BF16 && ctx->mttkrp_impl != 1 && R <= 128) ||
-         (t->dtype == PTG_F32 && R <= 64 && ctx->mttkrp_impl == 2);
+         (t->dtype == PTG_F32 && R <= 64 && ctx->mttkrp_impl != 1);
 }
 
 int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, int R, float *out,
@@ -444,7 +443,7 @@ int contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &c, 
   cudaEvent_t ev = nullptr;
   if (timed) PTG_TRY(stats_begin(ctx, stream, &ev));
   int rc;
-  const bool tc = contraction_uses_tc(ctx, t, R);
+  const bool tc = contraction_uses_tc(ctx, t, R) && !(c.exact_fp32 && t->dtype == PTG_F32);
   if (t->dtype == PTG_FP8E4M3)
     rc = f8_contraction_launch(ctx, t, c, R, out, stream);
   else if (t->dtype == PTG_F32 && tc)

@@ -16,8 +16,15 @@
 //   warp 1      TMEM allocation and the MMA issuer (one lane): per K-step of 8,
 //               D[:, 0:2N] += A_hi [K_hi; K_lo]^T and D[:, 0:N] += A_lo K_hi^T
 //               (M=128, N = R padded to 16), so A_hi is read once;
-//   warps 2..5  Khatri-Rao tiles ([hi rows; lo rows], swizzled K-major), then the TMEM drain
-//               (the two column halves summed) into split-K partials.
+//   warps 2..5  Khatri-Rao tiles ([hi rows; lo rows], swizzled K-major) and the drains of
+//               columns [0, N/2); warps 6..9 drain [N/2, N).
+// The tensor cores' FP32 accumulation in TMEM is not round-to-nearest: it drifts low by about
+// 2^-25 of the running sum per accumulate step, so a long chain carries a bias.  Every
+// accumulator chain therefore spans T3_CHAIN K-blocks (16 accumulate steps); the builders drain
+// it (the two column halves summed) into FP32 registers with round-to-nearest adds while the
+// MMA fills the other of two TMEM accumulators, and write the register sums as split-K
+// partials.  The builders and the splitters each keep half of the columns, so a CTA takes
+// 128/N q-tiles (between 2 and 8) with 64 sums per thread.
 // Every mbarrier wait is bounded: on timeout the kernel raises an error word, and returns
 // after its MMAs completed and its TMEM was released.
 #include <algorithm>
@@ -39,11 +46,45 @@ constexpr int T3_KSTAGES = 2;                  // Khatri-Rao ring: [hi rows; lo 
 constexpr int T3_TILE = T3_BM * T3_BK * 4;     // 16 KB
 constexpr int T3_THREADS = 320;
 constexpr uint32_t kTf32HiMask = 0xFFFFE000u;
-// K-blocks one CTA accumulates into its TMEM accumulator.  The accumulation drifts low by a
-// small relative amount per chained MMA, so the chain is cut into splits of at most this many
-// K-blocks (2048 terms); the split-K partials are summed in FP32 in split order, which is
-// unbiased.  At 1000^3 this makes ~500 splits instead of one per SM: 63 MB more partials.
-constexpr int64_t T3_CHAIN_KBLOCKS = 64;
+// K-blocks per TMEM accumulator chain before it is drained into FP32 registers
+constexpr int T3_CHAIN = 2;
+// q-tiles per CTA: the drained sums (MT x N/2 floats per thread) stay in registers, and the
+// two accumulators (2 x MT x 2N columns) fit the 512 columns of TMEM
+template <int N>
+struct T3Shape {
+  static constexpr int MT = 128 / N > 8 ? 8 : 128 / N;
+  static constexpr int HALF = N / 2;
+};
+
+// Chain c's accumulator, columns [col0, col0 + HALF) of both halves, added into the sums of
+// this thread's row (TMEM lanes 32 * quarter + lane); then the accumulator is released.
+template <int N>
+__device__ __forceinline__ bool t3_drain(float (&sum)[T3Shape<N>::MT][T3Shape<N>::HALF], int c, int nqt,
+                                         uint32_t tmem_base, int quarter, int col0, uint64_t *acc_full,
+                                         uint64_t *acc_empty, volatile int *abort_flag) {
+  constexpr int MT = T3Shape<N>::MT, HALF = T3Shape<N>::HALF;
+  const int buf = c & 1;
+  if (!mbar_wait(&acc_full[buf], (c >> 1) & 1, abort_flag)) return false;
+  tc_fence_after();
+#pragma unroll
+  for (int m = 0; m < MT; ++m) {
+    if (m < nqt) {
+#pragma unroll
+      for (int c0 = 0; c0 < HALF; c0 += 8) {
+        float v[8], w[8];
+        const uint32_t ta =
+            tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((buf * MT + m) * 2 * N + col0 + c0);
+        tmem_ld8(ta, v);
+        tmem_ld8(ta + (uint32_t)N, w);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) sum[m][c0 + i] += v[i] + w[i];
+      }
+    }
+  }
+  tc_fence_before();
+  mbar_arrive(&acc_empty[buf]);
+  return true;
+}
 
 struct T3Params {
   int64_t P, Q, S;
@@ -88,13 +129,14 @@ __device__ __forceinline__ void fail_timeout(volatile int *abort_flag, int *err)
   atomicExch(err, PTG_ERR_TIMEOUT);
 }
 
+template <int N>
 __global__ void __launch_bounds__(T3_THREADS, 1)
 mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm) {
+  constexpr int MT = T3Shape<N>::MT;
   if (prm.skip && *prm.skip) return;   // before any barrier or TMEM allocation
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const int N = prm.N;
-  const int KTILE = 2 * N * 128;                           // [hi rows 0..N-1; lo rows N..2N-1]
+  constexpr int KTILE = 2 * N * 128;                       // [hi rows 0..N-1; lo rows N..2N-1]
   uint8_t *xring = base;                                   // [8] staging tiles
   uint8_t *sring = xring + T3_XSTAGES * T3_TILE;           // [2]{hi, lo}
   uint8_t *kring = sring + T3_SSTAGES * 2 * T3_TILE;       // [2] Khatri-Rao tiles
@@ -102,7 +144,8 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
   uint64_t *full_x = bars, *free_x = bars + T3_XSTAGES;
   uint64_t *full_s = bars + 2 * T3_XSTAGES, *empty_s = full_s + T3_SSTAGES;
   uint64_t *full_k = empty_s + T3_SSTAGES, *empty_k = full_k + T3_KSTAGES;
-  uint64_t *done = empty_k + T3_KSTAGES;
+  uint64_t *acc_full = empty_k + T3_KSTAGES, *acc_empty = acc_full + 2;   // per accumulator
+  uint64_t *done = acc_empty + 2;
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
@@ -126,6 +169,10 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
     for (int i = 0; i < T3_KSTAGES; ++i) {
       mbar_init(&full_k[i], 128);
       mbar_init(&empty_k[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], 256);   // the builders and the splitters
     }
     mbar_init(done, 1);
     *abort_flag = 0;
@@ -178,7 +225,9 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
-    // per K-step of 8: D[:, 0:2N] += A_hi [K_hi; K_lo]^T, then D[:, 0:N] += A_lo K_hi^T
+    // per K-step of 8: D[:, 0:2N] += A_hi [K_hi; K_lo]^T, then D[:, 0:N] += A_lo K_hi^T; chain c
+    // (K-blocks c*T3_CHAIN ..) accumulates into accumulator c & 1, which its drain must have
+    // emptied (chain c - 2)
     if (lane == 0) {
       const uint32_t idesc2 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)((2 * N) >> 3) << 17) |
                               ((uint32_t)(T3_BM >> 4) << 24);
@@ -188,6 +237,14 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
       uint32_t sph = 0, kph = 0;
       bool ok = true;
       for (int kb = 0; kb < nkb && ok; ++kb) {
+        const int c = kb / T3_CHAIN, cs = kb - c * T3_CHAIN, buf = c & 1;
+        if (cs == 0 && c >= 2) {
+          if (!mbar_wait(&acc_empty[buf], ((c >> 1) - 1) & 1, abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+        }
         if (!mbar_wait(&full_k[ks], kph, abort_flag)) {
           ok = false;
           break;
@@ -201,13 +258,13 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
           }
           tc_fence_after();
           const uint32_t ahi = smem_u32(sring + ss * 2 * T3_TILE), alo = ahi + (uint32_t)T3_TILE;
-          const uint32_t d = tmem_base + (uint32_t)(m * 2 * N);
+          const uint32_t d = tmem_base + (uint32_t)((buf * MT + m) * 2 * N);
 #pragma unroll
           for (int kk = 0; kk < T3_BK / 8; ++kk) {
             const uint64_t adh = smem_desc_sw128(ahi + kk * 32, 16, 1024);
             const uint64_t adl = smem_desc_sw128(alo + kk * 32, 16, 1024);
             const uint64_t bd = smem_desc_sw128(kt + kk * 32, 16, 1024);   // 2N rows: hi then lo
-            umma_tf32(d, adh, bd, idesc2, (kb > 0 || kk > 0) ? 1u : 0u);
+            umma_tf32(d, adh, bd, idesc2, (cs > 0 || kk > 0) ? 1u : 0u);
             umma_tf32(d, adl, bd, idesc1, 1u);                              // first N rows: hi
           }
           umma_commit(&empty_s[ss]);
@@ -222,20 +279,36 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
           ks = 0;
           kph ^= 1;
         }
+        if (cs == T3_CHAIN - 1 || kb == nkb - 1) umma_commit(&acc_full[buf]);   // the chain is complete
       }
       if (!ok) fail_timeout(abort_flag, prm.err);
       umma_commit(done);   // arrives once every MMA issued above has completed
     }
   } else if (warp < 6) {
-    // ---------------- Khatri-Rao builders (128 threads) ----------------
+    // ---------------- Khatri-Rao builders and drains (128 threads) ----------------
     const int tb = threadIdx.x - 64;
     const int k = tb & 31, ng = tb >> 5;
-    const int cpg = N / 4;   // columns per group (>= 4)
+    constexpr int cpg = N / 4;   // columns per group (>= 4)
+    const int quarter = warp & 3;   // the TMEM lanes this warp may read: 32 * quarter ..
+    constexpr int HALF = T3Shape<N>::HALF;
+    float sum[MT][HALF];   // columns [0, HALF) of this thread's row
+#pragma unroll
+    for (int m = 0; m < MT; ++m)
+#pragma unroll
+      for (int i = 0; i < HALF; ++i) sum[m][i] = 0.0f;
+    bool alive = true;
+    auto drain = [&](int c) {
+      if (alive && !t3_drain<N>(sum, c, nqt, tmem_base, quarter, 0, acc_full, acc_empty, abort_flag)) {
+        fail_timeout(abort_flag, prm.err);
+        alive = false;
+      }
+    };
     int ks = 0;
     uint32_t kph = 0;
     for (int kb = 0; kb < nkb; ++kb) {
       if (!mbar_wait(&empty_k[ks], kph ^ 1, abort_flag)) {
         fail_timeout(abort_flag, prm.err);
+        alive = false;
         break;
       }
       const int64_t t = kb0 + kb;
@@ -286,37 +359,40 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
         ks = 0;
         kph ^= 1;
       }
+      // at the end of chain c, drain chain c - 1 (the MMA is filling chain c's accumulator)
+      const int c = kb / T3_CHAIN;
+      if ((kb - c * T3_CHAIN == T3_CHAIN - 1 || kb == nkb - 1) && c >= 1) drain(c - 1);
     }
-    // ---------------- epilogue: TMEM -> partials (the two column halves summed) ----------------
-    const bool have = (nkb > 0) && mbar_wait(done, 0, abort_flag) && !*abort_flag;
-    tc_fence_after();
-    const int quarter = warp & 3;
+    if (nkb > 0) drain((nkb - 1) / T3_CHAIN);
+    // ---------------- the drained sums -> split-K partials ----------------
     const int row = quarter * 32 + lane;
-    for (int m = 0; m < nqt; ++m) {
+#pragma unroll
+    for (int m = 0; m < MT; ++m) {
+      if (m >= nqt) continue;
       const int64_t q = (int64_t)(qt0 + m) * T3_BM + row;
+      if (q >= prm.Q) continue;
       float *dst = prm.partial + ((int64_t)split * prm.Q + q) * N;
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        float v[16], w[16];
-        if (have) {
-          const uint32_t ta = tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(m * 2 * N + c0);
-          tmem_ld16(ta, v);
-          tmem_ld16(ta + (uint32_t)N, w);
 #pragma unroll
-          for (int i = 0; i < 16; ++i) v[i] += w[i];
-        } else {
-#pragma unroll
-          for (int i = 0; i < 16; ++i) v[i] = 0.0f;
-        }
-        if (q < prm.Q) {
-#pragma unroll
-          for (int i = 0; i < 16; i += 4)
-            *reinterpret_cast<float4 *>(dst + c0 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-        }
-      }
+      for (int i = 0; i < HALF; i += 4)
+        *reinterpret_cast<float4 *>(dst + i) = make_float4(sum[m][i], sum[m][i + 1], sum[m][i + 2], sum[m][i + 3]);
     }
   } else {
-    // ---------------- X splitters (128 threads) ----------------
+    // ---------------- X splitters (128 threads), and the drains of columns [N/2, N) ----------------
     const int ts = threadIdx.x - 192;
+    const int quarter = warp & 3;
+    constexpr int HALF = T3Shape<N>::HALF;
+    float sum[MT][HALF];
+#pragma unroll
+    for (int m = 0; m < MT; ++m)
+#pragma unroll
+      for (int i = 0; i < HALF; ++i) sum[m][i] = 0.0f;
+    bool alive = true;
+    auto drain = [&](int c) {
+      if (alive && !t3_drain<N>(sum, c, nqt, tmem_base, quarter, HALF, acc_full, acc_empty, abort_flag)) {
+        fail_timeout(abort_flag, prm.err);
+        alive = false;
+      }
+    };
     int xs = 0, ss = 0;
     uint32_t xph = 0, sph = 0;
     for (int kb = 0; kb < nkb; ++kb) {
@@ -368,8 +444,24 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
           sph ^= 1;
         }
       }
+      // at the end of chain c, drain chain c - 1 (the MMA is filling chain c's accumulator)
+      const int c = kb / T3_CHAIN;
+      if ((kb - c * T3_CHAIN == T3_CHAIN - 1 || kb == nkb - 1) && c >= 1) drain(c - 1);
     }
+    alive = alive && !*abort_flag;
+    if (nkb > 0) drain((nkb - 1) / T3_CHAIN);
   split_done:;
+    const int row = quarter * 32 + lane;
+#pragma unroll
+    for (int m = 0; m < MT; ++m) {
+      if (m >= nqt) continue;
+      const int64_t q = (int64_t)(qt0 + m) * T3_BM + row;
+      if (q >= prm.Q) continue;
+      float *dst = prm.partial + ((int64_t)split * prm.Q + q) * N + HALF;
+#pragma unroll
+      for (int i = 0; i < HALF; i += 4)
+        *reinterpret_cast<float4 *>(dst + i) = make_float4(sum[m][i], sum[m][i + 1], sum[m][i + 2], sum[m][i + 3]);
+    }
   }
   // before TMEM is released and the CTA exits: every MMA has completed (the issuer's final
   // commit) and every TMA load this CTA issued has landed, waited for with a bound even
@@ -403,7 +495,7 @@ __global__ void tc32_reduce_kernel(const float *__restrict__ partial, int nsplit
 size_t tc32_smem_bytes(int N) {
   return 1024 /*alignment slack*/ + (size_t)T3_XSTAGES * T3_TILE + (size_t)T3_SSTAGES * 2 * T3_TILE +
          (size_t)T3_KSTAGES * 2 * N * 128 +
-         sizeof(uint64_t) * (2 * T3_XSTAGES + 2 * T3_SSTAGES + 2 * T3_KSTAGES + 1) + 16;
+         sizeof(uint64_t) * (2 * T3_XSTAGES + 2 * T3_SSTAGES + 2 * T3_KSTAGES + 4 + 1) + 16;
 }
 
 }  // namespace
@@ -439,14 +531,14 @@ int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction
   prm.before = cp(c.before);
   prm.after = cp(c.after);
   prm.qtiles = (int)((c.Q + T3_BM - 1) / T3_BM);
-  int mt = std::max(1, 512 / (2 * prm.N));   // TMEM: 2N columns per q-tile
-  mt = std::min(mt, prm.qtiles);
+  const int mt_max = std::min(8, 128 / prm.N);   // T3Shape<N>::MT
+  int mt = std::min(mt_max, prm.qtiles);
   const int qgroups_min = (prm.qtiles + mt - 1) / mt;
   mt = (prm.qtiles + qgroups_min - 1) / qgroups_min;   // balance q-tiles over the groups
   prm.mt_per_cta = mt;
   const int qgroups = (prm.qtiles + mt - 1) / mt;
-  uint32_t cols = 32;
-  while (cols < (uint32_t)(mt * 2 * prm.N)) cols <<= 1;
+  uint32_t cols = 32;   // two accumulators of MT q-tiles x 2N columns
+  while (cols < (uint32_t)(2 * mt_max * 2 * prm.N)) cols <<= 1;
   prm.tmem_cols = cols;
   if (mmajor) {
     prm.pblocks = 1;
@@ -456,7 +548,6 @@ int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction
     prm.kblocks_total = c.S * prm.pblocks;
   }
   int64_t nsplit = std::max<int64_t>(1, ctx->sm_count / qgroups);
-  nsplit = std::max<int64_t>(nsplit, (prm.kblocks_total + T3_CHAIN_KBLOCKS - 1) / T3_CHAIN_KBLOCKS);
   nsplit = std::min<int64_t>(nsplit, prm.kblocks_total);
   prm.kblocks_per_split = (prm.kblocks_total + nsplit - 1) / nsplit;
   nsplit = (prm.kblocks_total + prm.kblocks_per_split - 1) / prm.kblocks_per_split;
@@ -494,11 +585,15 @@ int tc32_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction
   prm.skip = c.skip;
   const size_t smem = tc32_smem_bytes(prm.N);
   if (smem > ctx->smem_optin) return set_error(PTG_ERR_UNSUPPORTED, "tensor-core FP32 MTTKRP: shared memory");
-  PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc32_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+  auto kern = prm.N == 16 ? mttkrp_tc32_kernel<16>
+              : prm.N == 32 ? mttkrp_tc32_kernel<32>
+              : prm.N == 48 ? mttkrp_tc32_kernel<48>
+                            : mttkrp_tc32_kernel<64>;
+  PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                 cudaSharedmemCarveoutMaxShared));
   dim3 grid((unsigned)qgroups, (unsigned)nsplit);
-  mttkrp_tc32_kernel<<<grid, T3_THREADS, smem, stream>>>(map, prm);
+  kern<<<grid, T3_THREADS, smem, stream>>>(map, prm);
   PTG_CUDA(cudaGetLastError());
   const int64_t n = c.q_write * R;
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->sm_count * 8);

@@ -38,12 +38,13 @@ def _bf16_round(X):
                                     ((40, 48, 56), 32), ((31, 17, 29), 40), ((20, 24, 18), 64),
                                     ((13, 12, 11), 100), ((7, 6, 5, 4), 3), ((10, 9, 8, 7), 33),
                                     ((5, 4, 3, 3, 2), 4)])
-def test_mttkrp_fp32_all_modes(pkg, ctx, dims, R):
+@pytest.mark.parametrize("impl", ["auto", "cuda_cores"])   # auto: the TF32 tensor cores at R <= 64
+def test_mttkrp_fp32_all_modes(pkg, ctx, dims, R, impl):
     rng = np.random.default_rng(sum(dims) + R)
     X = rng.standard_normal(dims)
     f = [rng.uniform(-1, 1, (I, R)) for I in dims]
     for mode in range(len(dims)):
-        got = _run(pkg, ctx, X, f, R, mode)
+        got = _run(pkg, ctx, X, f, R, mode, impl=impl)
         ref = oc.mttkrp(f, X, mode)
         err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
         assert err < 1e-5, (mode, err)

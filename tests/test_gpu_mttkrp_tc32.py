@@ -4,9 +4,10 @@ FP32 tensor).
 
 Bar: 1e-5 relative (Frobenius) at these contraction lengths (<= ~4e4 terms), within 5x the
 CUDA-core FP32 kernel's error; a single-term TF32 product would miss it by two orders of
-magnitude (TF32 keeps 10 mantissa bits).  The accumulation in TMEM is not unbiased: at
-1000^3 (1e6 terms per output) the error reaches ~1e-4, which is why the automatic selection
-keeps FP32 storage on the CUDA cores."""
+magnitude (TF32 keeps 10 mantissa bits).  The accumulation in TMEM is not round-to-nearest
+(it drifts low by ~2^-25 of the running sum per accumulate step), so the kernel drains each
+accumulator every two K-blocks into FP32 registers; at 10^6 terms per output the bias stays
+below 2e-6 relative."""
 import numpy as np
 import pytest
 
@@ -68,10 +69,10 @@ def test_cpd_fp32_tensor_cores_follows_oracle(pkg, ctx):
 def test_mttkrp_fp32_tensor_cores_long_contraction(pkg, ctx):
     """10^6 terms per output (mode 0 of 64 x 1000 x 1000, the contraction length of the
     1000^3 modes), uniform [0, 1) data and factors, so that a one-signed drift of the
-    accumulation cannot cancel.  The TMEM accumulation drifts low by ~2^-25 per accumulate
-    step; with each CTA's chain capped at 64 K-blocks (512 steps) the measured error is a
-    -1.9e-5 relative bias (it was ~-5e-5 uncapped).  The bound stated for this opt-in form:
-    3e-5 relative, all of it bias; the CUDA-core FP32 kernel stays the automatic choice."""
+    accumulation cannot cancel.  Each TMEM accumulator chain spans two K-blocks (16
+    accumulate steps, ~2^-25 drift each) before it is drained into FP32 registers, so the
+    relative bias stays below 2e-6 (it was -1.9e-5 with 64-K-block chains and ~-5e-5 with
+    one chain per CTA)."""
     rng = np.random.default_rng(11)
     dims, R = (64, 1000, 1000), 32
     X = rng.random(dims)
@@ -81,6 +82,7 @@ def test_mttkrp_fp32_tensor_cores_long_contraction(pkg, ctx):
         ref = oc.mttkrp(f, X, mode)
         err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
         bias = float(np.mean((got - ref) / ref))
-        assert err < 3e-5 and -3e-5 < bias < 1e-6, (mode, err, bias)
+        print(f"mode {mode}: error {err:.3e}, bias {bias:.3e}")
+        assert err < 4e-6 and -2e-6 < bias < 1e-6, (mode, err, bias)
         simt = _run(pkg, ctx, X, f, R, mode, impl="cuda_cores")
         assert np.linalg.norm(simt - ref) / np.linalg.norm(ref) < 1e-5, mode
