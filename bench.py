@@ -743,6 +743,7 @@ def run_gtc(args):
     vals_tr = vals[:n_train].contiguous()
     idx_ho, vals_ho, clean_ho = idx[:, n_train:], vals[n_train:], clean[n_train:]
     ctx = pkg.Context(0)
+    ctx.set_gtc_rows(args.gtc_rows)
     init = [np.random.default_rng(k).random((I, R)) for k, I in enumerate(dims)]
 
     def rmse(factors):
@@ -775,7 +776,7 @@ def run_gtc(args):
             "value": out["stochastic"]["observed_entries_per_s"], "unit": "entries/s", "n_gpus": 1,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic (uniform sample, rank-32 model, 10% noise)",
             "config": {"workload": "gtc_stochastic 50000x50000x5000", "nnz_train": n_train, "nnz_heldout": n_hold,
-                       "rank": R, "lambda": 1e-3, "c_stochastic_perc": args.gtc_c},
+                       "rank": R, "lambda": 1e-3, "c_stochastic_perc": args.gtc_c, "row_solver": args.gtc_rows},
             "runs": out, "heldout_rmse_noise_floor": floor, "cpu_baseline": cpu}
     print(json.dumps(line), flush=True)
     ctx.close()
@@ -915,6 +916,8 @@ def main():
     ap.add_argument("--gtc-epochs", type=int, default=2, help="stochastic GTC epochs (its max_iter)")
     ap.add_argument("--gtc-full-iters", type=int, default=2)
     ap.add_argument("--gtc-c", type=float, default=0.01, help="sampled fraction of each row per inner step")
+    ap.add_argument("--gtc-rows", default="auto", choices=["auto", "warp_fma", "cta"],
+                    help="row solver: auto (warp per row, Hessian on the tensor cores), warp_fma, cta")
     ap.add_argument("--gtc-cpu-entries", type=float, default=4e6, help="observed entries per mode the CPU baseline solves")
     ap.add_argument("--batch-sample", type=int, default=32, help="instances the CPU baseline solves")
     args = ap.parse_args()

@@ -84,8 +84,10 @@ typedef enum {
   PTG_OPT_NNLS_CLUSTER = 2 /* CTAs of the NNLS thread-block cluster: 0 auto (16 where the device
                              schedules it, else 8), or 2, 4, 8, 16 */,
   PTG_OPT_GTC_ROWS = 3 /* sparse row solver of the nonnegative GTC modes: 0 auto (one warp per
-                          row for rank <= 32, else one CTA per row), 1 one CTA per row; both
-                          give the same bits */,
+                          row for rank <= 32, the row Hessian on the tensor cores when rank % 4
+                          == 0 (TF32, three-term split); else one CTA per row), 1 one CTA per
+                          row, 2 one warp per row with the Hessian on the FMA pipe (the same
+                          bits as 1) */,
   PTG_OPT_SPIN_LIMIT = 4 /* polls of every bounded wait in the tensor-core MTTKRP kernels before
                             they give up with PTG_ERR_TIMEOUT: -1 the default (2^26), 0 give up
                             at once, before any copy or MMA is issued (a test of the failure

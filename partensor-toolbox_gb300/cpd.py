@@ -119,8 +119,11 @@ class Context:
 
     def set_gtc_rows(self, solver: str):
         """Row solver of the sparse completion's nonnegative modes: "auto" (one warp per row
-        for rank <= 32) or "cta" (one CTA per row); both give the same bits."""
-        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_GTC_ROWS, {"auto": 0, "cta": 1}[solver]))
+        for rank <= 32, the row Hessian on the tensor cores when rank % 4 == 0), "cta" (one
+        CTA per row) or "warp_fma" (one warp per row, the Hessian on the FMA pipe: the same
+        bits as "cta")."""
+        check(self._lib.ptg_ctx_set_option(self.handle, _lib.PTG_OPT_GTC_ROWS,
+                                           {"auto": 0, "cta": 1, "warp_fma": 2}[solver]))
 
     def set_spin_limit(self, polls: int):
         """Polls of the tensor-core kernels' bounded waits before they give up with

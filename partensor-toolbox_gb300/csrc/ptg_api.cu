@@ -332,7 +332,7 @@ int ptg_ctx_set_option(ptg_ctx *c, int option, long long value) {
       c->nnls_cluster = (int)value;   // 0: probe again on the next solve
       return PTG_OK;
     case PTG_OPT_GTC_ROWS:
-      if (value != 0 && value != 1) return set_error(PTG_ERR_INVALID, "GTC row solver must be 0 (auto) or 1");
+      if (value < 0 || value > 2) return set_error(PTG_ERR_INVALID, "GTC row solver must be 0 (auto), 1 or 2");
       c->gtc_rows = (int)value;
       return PTG_OK;
     case PTG_OPT_SPIN_LIMIT:

@@ -278,6 +278,7 @@ struct RowArgs {
   double *row_cost;        // optional: per-row sum of squared residuals with the new row
   int ridge;               // 1: unconstraint_update, a_i = (H_i + lambda I)^{-1} m_i
   int *err;                // device error word (a non-positive pivot in the ridge solve)
+  int tc;                  // warp solver: H_i on the tensor cores (TF32, three-term split)
 };
 
 // Hadamard of the other modes' factor rows for entry s, multiplied from the last mode down
@@ -649,7 +650,8 @@ __global__ void __launch_bounds__(GT_THREADS) gtc_row_kernel(const RowArgs a) {
 constexpr int GW_WARPS = 4;
 constexpr int GW_CHUNK = 32;
 
-constexpr int GW_KRS = 36;   // row stride of the Khatri-Rao staging (16-byte rows, rotated banks)
+constexpr int GW_KRS = 40;   // row stride of the Khatri-Rao staging: 16-byte rows, and the MMA
+                             // fragments' reads (rows t, t + 4; columns g) fall in distinct banks
 
 struct WarpRowShared {
   float kr[GW_CHUNK][GW_KRS];   // one entry's Khatri-Rao row per row; after a block, H_i by rows
@@ -805,6 +807,127 @@ __device__ __forceinline__ void warp_row_hessian(const RowArgs &a, WarpRowShared
   m = cg == 0 ? m4[0] : cg == 1 ? m4[1] : cg == 2 ? m4[2] : m4[3];   // m_i[lane]
 }
 
+// x rounded to TF32 (nearest, ties away), as the bits an mma.sync .tf32 operand takes
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// d += a b for one m16n8k8 tile (TF32 operands, FP32 accumulator)
+__device__ __forceinline__ void mma_tf32_16x8x8(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// warp_row_hessian with H_i = K^T K on the tensor cores (R <= 32, R % 4 == 0): K is the block's
+// entries x 32 Khatri-Rao rows staged in shared memory, eight entries per m16n8k8 step.  With
+// g = lane / 4 and t = lane % 4, the A fragment of K^T's rows 16 mt.. (K[e0 + t][16 mt + g],
+// K[e0 + t][16 mt + g + 8], K[e0 + t + 4][16 mt + g], K[e0 + t + 4][16 mt + g + 8]) also holds
+// the B fragments of K's columns 16 mt.. and 16 mt + 8.., so eight shared loads feed the six
+// tiles of the lower triangle's blocks (rows 0-15 x columns 0-15, rows 16-31 x columns 0-31);
+// the block above the diagonal is their transpose.  Each product is the three-term split
+// hi*hi + hi*lo + lo*hi of x = hi + lo (Markidis et al. 2018), so H_i keeps FP32 accuracy.
+// m_i[lane] = sum x_e K[e][lane] stays on the FMA pipe.
+template <int NJ>
+__device__ __forceinline__ void warp_row_hessian_mma(const RowArgs &a, WarpRowShared &sh, int64_t s1, int64_t nb,
+                                                     float (&H)[32], float &m) {
+  const int lane = threadIdx.x & 31, R = a.R;
+  const int g = lane >> 2, t = lane & 3;
+  float acc[6][4];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+  float mv = 0.0f;
+  for (int64_t s0 = s1; s0 < s1 + nb; s0 += GW_CHUNK) {
+    const int cnt = (int)(s1 + nb - s0 < GW_CHUNK ? s1 + nb - s0 : GW_CHUNK);
+    const int cnt8 = (cnt + 7) & ~7;
+    if (lane < cnt) {
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) sh.rows[j][lane] = a.oidx[(int64_t)j * a.nnz + s0 + lane];
+      sh.xv[lane] = a.vals[s0 + lane];
+    }
+    __syncwarp();
+    {   // each entry's Khatri-Rao row (the product from the last mode down); ranks >= R and the
+        // rows that pad the chunk to a multiple of eight entries are zero
+      const int sub = lane >> 3, r4 = (lane & 7) * 4;
+#pragma unroll 2
+      for (int e = sub; e < cnt8; e += 4) {
+        float4 kv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (e < cnt && r4 < R) {
+          kv = __ldg(reinterpret_cast<const float4 *>(a.fac[NJ - 1] + (size_t)sh.rows[NJ - 1][e] * R + r4));
+#pragma unroll
+          for (int j = NJ - 2; j >= 0; --j) {
+            const float4 f = __ldg(reinterpret_cast<const float4 *>(a.fac[j] + (size_t)sh.rows[j][e] * R + r4));
+            kv.x *= f.x;
+            kv.y *= f.y;
+            kv.z *= f.z;
+            kv.w *= f.w;
+          }
+        }
+        *reinterpret_cast<float4 *>(&sh.kr[e][r4]) = kv;
+      }
+    }
+    __syncwarp();
+    for (int e = 0; e < cnt; ++e) mv = fmaf(sh.xv[e], sh.kr[e][lane], mv);
+    for (int e0 = 0; e0 < cnt8; e0 += 8) {
+      uint32_t hi[2][4], lo[2][4];
+#pragma unroll
+      for (int mt = 0; mt < 2; ++mt) {
+        const float x[4] = {sh.kr[e0 + t][16 * mt + g], sh.kr[e0 + t][16 * mt + g + 8], sh.kr[e0 + t + 4][16 * mt + g],
+                            sh.kr[e0 + t + 4][16 * mt + g + 8]};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          hi[mt][i] = tf32_rna(x[i]);
+          lo[mt][i] = tf32_rna(x[i] - __uint_as_float(hi[mt][i]));
+        }
+      }
+      // tile (mt, nt): rows 16 mt.., columns 8 nt..; B of columns 8 nt.. is A fragment nt / 2's
+      // elements (nt & 1, (nt & 1) + 2)
+#pragma unroll
+      for (int tile = 0; tile < 6; ++tile) {
+        const int mt = tile < 2 ? 0 : 1, nt = tile < 2 ? tile : tile - 2;
+        const int bm = nt >> 1, bh = nt & 1;
+        mma_tf32_16x8x8(acc[tile], hi[mt], hi[bm][bh], hi[bm][bh + 2]);
+        mma_tf32_16x8x8(acc[tile], hi[mt], lo[bm][bh], lo[bm][bh + 2]);
+        mma_tf32_16x8x8(acc[tile], lo[mt], hi[bm][bh], hi[bm][bh + 2]);
+      }
+    }
+    __syncwarp();   // the staging buffer is gathered into again by the next chunk
+  }
+  // H_i through the staging buffer: each tile's elements, and the transposes of the tiles
+  // below the diagonal blocks; then lane r takes row r
+#pragma unroll
+  for (int tile = 0; tile < 6; ++tile) {
+    const int mt = tile < 2 ? 0 : 1, nt = tile < 2 ? tile : tile - 2;
+    const int r0 = 16 * mt + g, c0 = 8 * nt + 2 * t;
+    sh.kr[r0][c0] = acc[tile][0];
+    sh.kr[r0][c0 + 1] = acc[tile][1];
+    sh.kr[r0 + 8][c0] = acc[tile][2];
+    sh.kr[r0 + 8][c0 + 1] = acc[tile][3];
+    if (mt == 1 && nt < 2) {
+      sh.kr[c0][r0] = acc[tile][0];
+      sh.kr[c0 + 1][r0] = acc[tile][1];
+      sh.kr[c0][r0 + 8] = acc[tile][2];
+      sh.kr[c0 + 1][r0 + 8] = acc[tile][3];
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const float4 v = *reinterpret_cast<const float4 *>(&sh.kr[lane][4 * q]);
+    H[4 * q] = v.x;
+    H[4 * q + 1] = v.y;
+    H[4 * q + 2] = v.z;
+    H[4 * q + 3] = v.w;
+  }
+  __syncwarp();
+  m = mv;
+}
+
 // one projected Nesterov step of this lane's column: grad = H y - m + lambda (y + prox a)
 __device__ __forceinline__ void warp_row_step(const float (&H)[32], float *v, float m, bool own, float lam,
                                               float invL, float beta, float prox, float &av, float &yv) {
@@ -821,8 +944,8 @@ __device__ __forceinline__ void warp_row_step(const float (&H)[32], float *v, fl
 // STOCH: dynamic_blocksize::StochasticNesterovMNLS, a fresh sampled block per inner step;
 // else local_L::NesterovMNLS, H_i over all the row's entries, then max_iter steps
 // (nonnegative modes; the ridge solve of unconstrained modes stays on the one-CTA kernel).
-template <int NJ, bool VEC, bool STOCH>
-__global__ void __launch_bounds__(GW_WARPS * 32, 7) gtc_warp_kernel(const RowArgs a, int64_t rows) {
+template <int NJ, bool VEC, bool STOCH, bool MMA = false>
+__global__ void __launch_bounds__(GW_WARPS * 32, MMA ? 6 : 7) gtc_warp_kernel(const RowArgs a, int64_t rows) {
   __shared__ __align__(16) WarpRowShared shw[GW_WARPS];
   const int lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * GW_WARPS + (threadIdx.x >> 5);
@@ -842,7 +965,8 @@ __global__ void __launch_bounds__(GW_WARPS * 32, 7) gtc_warp_kernel(const RowArg
                                                       (unsigned long long)a.mode, (unsigned long long)it,
                                                       (unsigned long long)i);
         const int64_t s1 = p0 + (int64_t)(draw % (unsigned long long)(cnt_row - b + 1));
-        warp_row_hessian<NJ, VEC>(a, sh, s1, b, H, m);
+        if constexpr (MMA) warp_row_hessian_mma<NJ>(a, sh, s1, b, H, m);
+        else warp_row_hessian<NJ, VEC>(a, sh, s1, b, H, m);
         float invL, beta;
         step_constants(power_method_lane(H, sh.v, own, 1e-3f), a.lambda, invL, beta);
         // grad = sum (kr.y - x) kr + lambda (y + a) = H y - m + lambda (y + a)
@@ -851,7 +975,8 @@ __global__ void __launch_bounds__(GW_WARPS * 32, 7) gtc_warp_kernel(const RowArg
       }
     }
   } else {
-    warp_row_hessian<NJ, VEC>(a, sh, p0, cnt_row, H, m);   // an empty row: H = 0, m = 0
+    if constexpr (MMA) warp_row_hessian_mma<NJ>(a, sh, p0, cnt_row, H, m);   // an empty row: H = 0, m = 0
+    else warp_row_hessian<NJ, VEC>(a, sh, p0, cnt_row, H, m);
     float invL, beta;
     step_constants(cnt_row > 0 ? power_method_lane(H, sh.v, own, 1e-3f) : 0.0f, a.lambda, invL, beta);
     for (int it = 0; it < a.max_iter; ++it) warp_row_step(H, sh.v, m, own, a.lambda, invL, beta, 0.0f, av, yv);
@@ -864,10 +989,12 @@ void launch_warp_rows_nj(const RowArgs &a, int64_t rows, cudaStream_t S) {
   const unsigned grid = (unsigned)((rows + GW_WARPS - 1) / GW_WARPS);
   const bool vec = a.R % 4 == 0;
   if (a.stochastic) {
-    if (vec) gtc_warp_kernel<NJ, true, true><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+    if (vec && a.tc) gtc_warp_kernel<NJ, true, true, true><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+    else if (vec) gtc_warp_kernel<NJ, true, true><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
     else gtc_warp_kernel<NJ, false, true><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
   } else {
-    if (vec) gtc_warp_kernel<NJ, true, false><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+    if (vec && a.tc) gtc_warp_kernel<NJ, true, false, true><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
+    else if (vec) gtc_warp_kernel<NJ, true, false><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
     else gtc_warp_kernel<NJ, false, false><<<grid, GW_WARPS * 32, 0, S>>>(a, rows);
   }
 }
@@ -1215,7 +1342,10 @@ int ptg_gtc(ptg_ctx *ctx, int order, const int64_t *dims, int64_t nnz, const int
       RowArgs a = make_args(n);
       a.outer = ao_iter;
       a.ridge = ridge ? 1 : 0;
-      if (R <= 32 && !a.ridge && ctx->gtc_rows == 0)
+      // row solvers: 0 auto (one warp per row at R <= 32, H_i on the tensor cores where
+      // R % 4 == 0), 1 one CTA per row, 2 one warp per row with H_i on the FMA pipe
+      a.tc = ctx->gtc_rows == 0 ? 1 : 0;
+      if (R <= 32 && !a.ridge && ctx->gtc_rows != 1)
         launch_warp_rows(a, dims[n], S);
       else
         gtc_row_kernel<<<(unsigned)dims[n], GT_THREADS, smem, S>>>(a);

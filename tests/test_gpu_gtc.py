@@ -121,14 +121,15 @@ def test_gtc_stochastic_keeps_unconstrained_modes(pkg, ctx):
 
 @pytest.mark.parametrize("R", [3, 17, 32])
 def test_gtc_stochastic_row_solvers_agree(pkg, ctx, R):
-    """The stochastic row solver with one warp per row (rank <= 32: H_i in the lanes' registers)
-    and the one with one CTA per row do the same arithmetic in the same order: same bits."""
+    """The stochastic row solver with one warp per row (rank <= 32: H_i in the lanes' registers,
+    formed on the FMA pipe) and the one with one CTA per row do the same arithmetic in the same
+    order: same bits."""
     dims = (70, 60, 50)
     idx, vals, init = _problem(dims, 30000, R, 21)
     o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=2, c_stochastic_perc=0.05,
                           lambdas=[1e-3] * 3, seed=3, factorsInit=init)
     out = {}
-    for solver in ("auto", "cta"):
+    for solver in ("warp_fma", "cta"):
         c = pkg.Context(0)
         try:
             c.set_gtc_rows(solver)
@@ -136,8 +137,8 @@ def test_gtc_stochastic_row_solvers_agree(pkg, ctx, R):
         finally:
             c.close()
     for k in range(3):
-        assert np.array_equal(out["auto"].factors[k], out["cta"].factors[k]), k
-    assert out["auto"].rel_costFunction == out["cta"].rel_costFunction
+        assert np.array_equal(out["warp_fma"].factors[k], out["cta"].factors[k]), k
+    assert out["warp_fma"].rel_costFunction == out["cta"].rel_costFunction
 
 
 @pytest.mark.parametrize("R", [3, 17, 32])
@@ -149,7 +150,7 @@ def test_gtc_full_row_solvers_agree(pkg, ctx, R):
     o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=3, lambdas=[1e-3] * 3,
                           factorsInit=init)
     out = {}
-    for solver in ("auto", "cta"):
+    for solver in ("warp_fma", "cta"):
         c = pkg.Context(0)
         try:
             c.set_gtc_rows(solver)
@@ -157,8 +158,8 @@ def test_gtc_full_row_solvers_agree(pkg, ctx, R):
         finally:
             c.close()
     for k in range(3):
-        assert np.array_equal(out["auto"].factors[k], out["cta"].factors[k]), k
-    assert out["auto"].rel_costFunction == out["cta"].rel_costFunction
+        assert np.array_equal(out["warp_fma"].factors[k], out["cta"].factors[k]), k
+    assert out["warp_fma"].rel_costFunction == out["cta"].rel_costFunction
 
 
 @pytest.mark.parametrize("R", [32, 40])
@@ -194,7 +195,7 @@ def test_gtc_4way_row_solvers(pkg, ctx, R):
         o = pkg.SparseOptions(order=4, rank=R, tnsDims=list(dims), max_iter=3, lambdas=[1e-3] * 4,
                               c_stochastic_perc=0.2, seed=7, factorsInit=init)
         out = {}
-        for solver in ("auto", "cta"):
+        for solver in ("warp_fma", "cta"):
             c = pkg.Context(0)
             try:
                 c.set_gtc_rows(solver)
@@ -202,9 +203,34 @@ def test_gtc_4way_row_solvers(pkg, ctx, R):
             finally:
                 c.close()
         for k in range(4):
-            assert np.array_equal(out["auto"].factors[k], out["cta"].factors[k]), (stochastic, k)
+            assert np.array_equal(out["warp_fma"].factors[k], out["cta"].factors[k]), (stochastic, k)
         if not stochastic:
             ref = og.gtc(idx, vals, dims, R, og.SparseOptions(order=4, max_iter=3, lambdas=[1e-3] * 4), init)
-            rel_gpu = np.array([t["rel"] for t in out["auto"].trace])
+            rel_gpu = np.array([t["rel"] for t in out["warp_fma"].trace])
             rel_ref = np.array([t["rel"] for t in ref.trace])
             assert np.max(np.abs(rel_gpu - rel_ref)) < 2e-4, (rel_gpu, rel_ref)
+
+
+@pytest.mark.parametrize("R", [8, 16, 32])
+def test_gtc_tensor_core_hessian_matches_fma(pkg, ctx, R):
+    """The default warp solver forms H_i on the tensor cores (mma.sync TF32, three-term split):
+    the local_L solve equals the FMA-pipe warp solver's up to FP32 summation order.  (The
+    stochastic form is compared with the oracle elsewhere: on problems this small its result
+    moves by ~0.02 in rel under a 1e-6 perturbation of the initial factors on either path, as
+    its power method stops at a 1e-3 tolerance, so two summation orders need not agree.)"""
+    dims = (70, 60, 50)
+    idx, vals, init = _problem(dims, 30000, R, 29)
+    o = pkg.SparseOptions(order=3, rank=R, tnsDims=list(dims), max_iter=2, lambdas=[1e-3] * 3, seed=3,
+                          factorsInit=init)
+    out = {}
+    for solver in ("auto", "warp_fma"):
+        c = pkg.Context(0)
+        try:
+            c.set_gtc_rows(solver)
+            out[solver] = pkg.gtc_coo(idx, vals, o, stochastic=False, ctx=c)
+        finally:
+            c.close()
+    for k in range(3):
+        a, b = out["auto"].factors[k], out["warp_fma"].factors[k]
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-4, k
+    assert abs(out["auto"].rel_costFunction - out["warp_fma"].rel_costFunction) < 1e-5
