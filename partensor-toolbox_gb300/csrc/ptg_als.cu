@@ -283,6 +283,14 @@ struct Runner {
     if (grams_ready) PTG_CUDA(cudaStreamWaitEvent(S, grams_ready, 0));
     PTG_TRY(launch_cost_terms(b.M, factors[0], b.rows[0], grams, b.N, b.R, b.dsc + 2,
                               CostScratch{b.cpart, b.cticket}, S));
+    // the exact fit: the Gram term from FP64 Grams of the factors (the FP32 Grams' rounding,
+    // ~1e-7 of ||X||^2, would move f^2 = ||X||^2 - 2<M, A> + ... by ~1e-7 / rel^2 of itself)
+    if (exact) {
+      PTG_TRY(ctx->scratch.ensure(sizeof(double) * gram_term_fp64_scratch_doubles(b.N, b.R)));
+      PTG_TRY(launch_gram_term_fp64(factors, b.rows, b.N, b.R, reinterpret_cast<double *>(ctx->scratch.ptr),
+                                    b.dsc + 3, S));
+      count_launches(ctx, 2);
+    }
     count_launches(ctx, 1);
     return PTG_OK;
   }

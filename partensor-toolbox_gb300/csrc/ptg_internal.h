@@ -346,6 +346,11 @@ struct CostScratch {
 constexpr int kCostPartials = 64;
 int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const float *const *grams,
                       int order, int R, double *out2, CostScratch scratch, cudaStream_t stream);
+// *out = sum over (r1, r2) of prod_k (A_k^T A_k)[r1][r2], the Grams accumulated in FP64 from the
+// factors (part: gram_term_fp64_scratch_doubles(order, R) doubles of scratch)
+size_t gram_term_fp64_scratch_doubles(int order, int R);
+int launch_gram_term_fp64(const float *const *factors, const int *rows, int order, int R, double *part,
+                          double *out, cudaStream_t stream);
 
 // Batched many-instance CPD (ptg_batched.cu, ptg_solve.cu).
 struct EigDesc {            // eigenbounds of one instance and mode

@@ -35,8 +35,10 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
 // ------------------------------------------------------------------------------------
 // Row-batched Nesterov MNLS on one cluster.
 // ------------------------------------------------------------------------------------
-constexpr int kNnlsWarps = 16;
-constexpr int kNnlsThreads = kNnlsWarps * 32;
+// Warps per CTA of the NNLS cluster kernel (its template parameter W).  16 warps (512 threads,
+// at most 128 registers each, a few spilled at 4+ rows per warp) measured faster than 8 warps
+// without spills: 1000^3 BF16 solve 30.4 vs 30.8 ms.
+constexpr int kNnlsWarpsLarge = 16;
 constexpr int kNnlsWindowMax = 8;
 
 struct NnlsArgs {
@@ -58,8 +60,9 @@ struct NnlsArgs {
   int window;            // iterations per cluster barrier, 1..kNnlsWindowMax (launch sets it)
 };
 
-template <int RB, int ROWS>
-__global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const NnlsArgs a) {
+template <int RB, int ROWS, int W>
+__global__ void __launch_bounds__(W * 32, 1) nnls_cluster_kernel(const NnlsArgs a) {
+  constexpr int kNnlsWarps = W;
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
@@ -457,28 +460,28 @@ __global__ void __launch_bounds__(kNnlsThreads, 1) nnls_cluster_kernel(const Nnl
   cluster.sync();   // keep every CTA's shared memory alive until rank 0 has read it
 }
 
-template <int RB, int ROWS>
+template <int RB, int ROWS, int kNnlsWarps>
 size_t nnls_smem_bytes(int R, int window) {
   return sizeof(float) * (2 * R * R + (size_t)window * kNnlsWarps * ROWS * R + ((R + 1) & ~1) + 4 + 2 * kNnlsWarps) +
          sizeof(double) * (kNnlsWarps + 2) + sizeof(int) * (8 + 3 * kNnlsWindowMax) +
          sizeof(float) * (kMaxInner + kNnlsWarps * ROWS) + (RB == 1 ? 16 + sizeof(float) * kNnlsWarps * ROWS * 32 : 0);
 }
 
-template <int RB, int ROWS>
+template <int RB, int ROWS, int kNnlsWarps>
 int launch_nnls_t(int cs, const NnlsArgs &args_in, cudaStream_t stream) {
-  auto kern = nnls_cluster_kernel<RB, ROWS>;
+  auto kern = nnls_cluster_kernel<RB, ROWS, kNnlsWarps>;
   // as many iterations per cluster barrier as the A_it slots fit in 96 KB (at most 8)
   NnlsArgs args = args_in;
   const size_t slot = sizeof(float) * kNnlsWarps * ROWS * args.R;
   args.window = (int)std::max<size_t>(1, std::min<size_t>(kNnlsWindowMax, (96u << 10) / slot));
-  const size_t smem = nnls_smem_bytes<RB, ROWS>(args.R, args.window);
+  const size_t smem = nnls_smem_bytes<RB, ROWS, kNnlsWarps>(args.R, args.window);
   PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (cs > 8) PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   if ((int64_t)cs * kNnlsWarps * ROWS < args.I)
     return set_error(PTG_ERR_INVALID, "internal: NNLS row tiling");
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cs, 1, 1);
-  cfg.blockDim = dim3(kNnlsThreads, 1, 1);
+  cfg.blockDim = dim3(kNnlsWarps * 32, 1, 1);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = stream;
   cudaLaunchAttribute attr[1];
@@ -497,13 +500,13 @@ int launch_nnls_t(int cs, const NnlsArgs &args_in, cudaStream_t stream) {
 int nnls_cluster_size(ptg_ctx *ctx) {
   if (ctx->nnls_cluster) return ctx->nnls_cluster;
   int cs = 8;
-  auto kern = nnls_cluster_kernel<2, 16>;
-  const size_t smem = nnls_smem_bytes<2, 16>(kMaxR, 1);   // the largest slot: one step per window
+  auto kern = nnls_cluster_kernel<2, 16, kNnlsWarpsLarge>;
+  const size_t smem = nnls_smem_bytes<2, 16, kNnlsWarpsLarge>(kMaxR, 1);   // the largest slot: one step per window
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess &&
       cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(16, 1, 1);
-    cfg.blockDim = dim3(kNnlsThreads, 1, 1);
+    cfg.blockDim = dim3(kNnlsWarpsLarge * 32, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -585,13 +588,13 @@ int launch_nnls_full(ptg_ctx *ctx, const float *M, float *A, int I, int R, const
   NnlsArgs args{M, A, I, R, np, delta1, delta2, gram_out, inner_MA, had_ZG, iters_out, repaired_out,
                 warm.theta, warm.hidden, warm.log_X, warm.log_T};
   const int cs = nnls_cluster_size(ctx);
-  const int cap = cs * kNnlsWarps;   // rows per register slot
-  const int rows = (I + cap - 1) / cap;
   const bool wide = R > 32;
-#define PTG_NNLS_CASE(RWS)                                                    \
-  if (rows <= RWS)                                                            \
-    return wide ? launch_nnls_t<2, RWS>(cs, args, stream)                     \
-                : launch_nnls_t<1, RWS>(cs, args, stream);
+  const int cap = cs * kNnlsWarpsLarge;   // rows per register slot
+  const int rows = (I + cap - 1) / cap;
+#define PTG_NNLS_CASE(RWS)                                                                        \
+  if (rows <= RWS)                                                                                \
+    return wide ? launch_nnls_t<2, RWS, kNnlsWarpsLarge>(cs, args, stream)                        \
+                : launch_nnls_t<1, RWS, kNnlsWarpsLarge>(cs, args, stream);
   PTG_NNLS_CASE(1)
   PTG_NNLS_CASE(2)
   PTG_NNLS_CASE(4)
@@ -801,6 +804,67 @@ int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const
   for (int k = 0; k < order; ++k) gp.g[k] = grams[k];
   cost_terms_kernel<<<kCostBlocks, kCostThreads, 0, stream>>>(M, A_last, I_last * R, gp, order, R, scratch.part,
                                                              scratch.ticket, out2);
+  PTG_CUDA(cudaGetLastError());
+  return PTG_OK;
+}
+
+namespace {
+struct FacPtrs {
+  const float *a[PTG_MAX_ORDER];
+  int rows[PTG_MAX_ORDER];
+};
+constexpr int kGramParts = 16;
+
+// Grams accumulated in FP64 from the factors: CTA (r1, k, p) and thread r2 sum
+// A_k[i][r1] A_k[i][r2] over the p-th contiguous share of the rows, into
+// part[((k * kGramParts + p) * R + r1) * R + r2]
+__global__ void gram_fp64_part_kernel(FacPtrs f, int R, double *part) {
+  const int r1 = blockIdx.x, k = blockIdx.y, p = blockIdx.z, r2 = threadIdx.x;
+  if (r2 >= R) return;
+  const int rows = f.rows[k], share = (rows + kGramParts - 1) / kGramParts;
+  const int i0 = p * share, i1 = min(rows, i0 + share);
+  const float *A = f.a[k];
+  double g = 0.0;
+  for (int i = i0; i < i1; ++i) g = fma((double)A[(size_t)i * R + r1], (double)A[(size_t)i * R + r2], g);
+  part[(((size_t)k * kGramParts + p) * R + r1) * R + r2] = g;
+}
+
+// *out = sum over (r1, r2) of prod_k G_k[r1][r2], the parts of each Gram added in order and the
+// pairs summed in a fixed order (one CTA of 1024 threads)
+__global__ void gram_term_fp64_kernel(const double *part, int order, int R, double *out) {
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int idx = threadIdx.x; idx < R * R; idx += blockDim.x) {
+    double prod = 1.0;
+    for (int k = order - 1; k >= 0; --k) {
+      double g = 0.0;
+      for (int p = 0; p < kGramParts; ++p) g += part[((size_t)k * kGramParts + p) * R * R + idx];
+      prod *= g;
+    }
+    s += prod;
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) *out = v;
+  }
+}
+}  // namespace
+
+size_t gram_term_fp64_scratch_doubles(int order, int R) { return (size_t)order * kGramParts * R * R; }
+
+int launch_gram_term_fp64(const float *const *factors, const int *rows, int order, int R, double *part,
+                          double *out, cudaStream_t stream) {
+  FacPtrs f{};
+  for (int k = 0; k < order; ++k) {
+    f.a[k] = factors[k];
+    f.rows[k] = rows[k];
+  }
+  gram_fp64_part_kernel<<<dim3(R, order, kGramParts), ((R + 31) / 32) * 32, 0, stream>>>(f, R, part);
+  gram_term_fp64_kernel<<<1, 1024, 0, stream>>>(part, order, R, out);
   PTG_CUDA(cudaGetLastError());
   return PTG_OK;
 }

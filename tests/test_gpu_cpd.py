@@ -186,11 +186,15 @@ def test_cpd_dimtree_3way(pkg, ctx):
 
 def test_cpd_bf16_verify_fp32_reports_fp32_cost(pkg, ctx):
     """verify_fp32: after a BF16 main loop the reported cost is the final factors' cost on the
-    FP32 copy (one MTTKRP), so it equals the FP64 residual of the returned factors."""
+    FP32 copy (one CUDA-core FP32 MTTKRP, the Gram term from FP64 Grams), so it equals the FP64
+    residual of the returned factors to what FP32 arithmetic allows.  The Gram form cancels:
+    f^2 = ||X||^2 - 2<M, A> + ..., with f^2 ~ 1e-3 ||X||^2 at 30 dB, so a relative error e of
+    the FP32 <M, A> moves f by ~1100 e; the bar, 5e-5 on f, is e < 4.5e-8, below FP32's unit
+    roundoff (6e-8)."""
     X, A, init = _cfg1_like((48, 40, 36), 6, seed=6, snr_db=30.0)
     st = pkg.cpd(X, 6, pkg.Options(order=3, max_iter=12, precision="bf16", verify_fp32=True), init, ctx=ctx)
     assert st.refine_sweeps_done == 0
-    assert oc.cost_from_factors(X, st.factors) == pytest.approx(st.f_value, rel=1e-5)
+    assert oc.cost_from_factors(X, st.factors) == pytest.approx(st.f_value, rel=5e-5)
     plain = pkg.cpd(X, 6, pkg.Options(order=3, max_iter=12, precision="bf16"), init, ctx=ctx)
     # the same factors; only where the cost is measured differs
     for k in range(3):
