@@ -125,3 +125,24 @@ def test_persistent_and_graph_solvers_agree(pkg, ctx, impl):
         assert a.ao_iter == b.ao_iter == 30
         assert a.rel_costFunction == pytest.approx(b.rel_costFunction, abs=2e-5)
         assert oc.congruence(a.factors, b.factors) >= 0.999
+
+
+def test_batched_order4_matches_single_path(pkg, ctx, impl):
+    """A batch of 4-way instances (the solvers take orders 3-8): the same sweeps as the single-
+    instance path, the fit within 1e-4 of it and within 1e-3 of the FP64 oracle."""
+    probs = []
+    for s, (dims, R) in enumerate([((12, 10, 9, 8), 3), ((9, 14, 7, 10), 5), ((16, 8, 8, 6), 4)]):
+        rng = np.random.default_rng(40 + s)
+        A = [rng.random((I, R)) for I in dims]
+        X = np.einsum("ir,jr,kr,lr->ijkl", *A)
+        X = X + 0.05 * np.sqrt((X ** 2).mean()) * rng.standard_normal(dims)
+        init = [np.random.default_rng(140 + s).random((I, R)) for I in dims]
+        probs.append((X, R, init))
+    opts = pkg.Options(order=4, max_iter=12)
+    sts, _ = pkg.cpd_batched(probs, opts, ctx=ctx)
+    for (X, R, init), st in zip(probs, sts):
+        one = pkg.cpd(X, R, opts, init, ctx=ctx)
+        assert st.ao_iter == one.ao_iter == 12
+        assert st.rel_costFunction == pytest.approx(one.rel_costFunction, abs=1e-4)
+        ref = oc.cpd_als(X, R, oc.Options(order=4, max_iter=12), init)
+        assert abs(st.rel_costFunction - ref.rel_costFunction) < 1e-3
