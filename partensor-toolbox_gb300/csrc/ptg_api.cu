@@ -251,6 +251,11 @@ int ptg_ctx_create(int device, ptg_ctx **out) {
   c->cc_major = prop.major;
   c->cc_minor = prop.minor;
   c->smem_optin = prop.sharedMemPerBlockOptin;
+  {
+    const size_t eig = eigen_kernel_smem() + prop.reservedSharedMemPerBlock;
+    const size_t avail = prop.sharedMemPerMultiprocessor - prop.reservedSharedMemPerBlock;
+    c->smem_beside_eigen = std::min(c->smem_optin, avail > eig ? avail - eig : (size_t)0);
+  }
   int pageable = 0, host_tables = 0;
   if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess ||
       cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess) {

@@ -217,8 +217,9 @@ using namespace tc;
 
 constexpr int F8_BM = 128;          // q rows per tile (MMA M)
 constexpr int F8_BK = 128;          // contraction elements per K-block (one 128-byte row)
-constexpr int F8_MAX_STAGES = 8;    // X tile ring
-constexpr int F8_MAX_KSTAGES = 4;   // Khatri-Rao tile ring
+constexpr int F8_MAX_STAGES = 6;    // X tile ring (measured faster than 8 to 10)
+constexpr int F8_GROUP = 2;         // K-blocks per group, modes n >= 1 (measured: 2 beats 1 and 4)
+constexpr int F8_MAX_KSTAGES = 4;   // Khatri-Rao tile ring: two groups
 constexpr int F8_THREADS = 320;     // producer, MMA issuer, 8 Khatri-Rao builder warps
 constexpr int F8_BUILDERS = 256;
 constexpr int F8_ATILE = F8_BM * F8_BK;   // 16 KB
@@ -233,6 +234,7 @@ struct F8Params {
   int R;
   int mmajor;
   int stages, kstages;
+  int group;                 // G: K-blocks per group; the q-tiles are the outer loop of a group
   uint32_t tmem_cols;
   uint32_t spin;             // poll limit of every bounded wait
   int vec4;                  // factor rows are read as float4 (R % 4 == 0, 16-byte aligned)
@@ -302,7 +304,7 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int N = prm.N, RP = prm.RP;
-  const int STAGES = prm.stages, KSTAGES = prm.kstages;
+  const int STAGES = prm.stages, KSTAGES = prm.kstages, G = prm.group;
   const int KTILE = N * 128;   // N rows of 128 bytes
   uint8_t *aring = base;
   uint8_t *kring = aring + STAGES * F8_ATILE;
@@ -364,27 +366,71 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
       uint32_t phase = 0;
       int issued[F8_MAX_STAGES] = {0};   // loads issued into each stage
       bool ok = true;
-      for (int kb = 0; kb < nkb && ok; ++kb) {
-        const int64_t t = kb0 + kb;
-        for (int m = 0; m < nqt; ++m) {
-          if (!mbar_wait_lim(&empty_a[stage], phase ^ 1, abort_flag, spin)) {
-            ok = false;
-            break;
+      // K-block t covers s in [t BK, t BK + BK) (mode 0), else slab t / pblocks, p from
+      // (t % pblocks) BK; the coordinates step along a group without dividing
+      const int pend = (int)(prm.pblocks * F8_BK);
+      if (G == 1) {   // one K-block at a time (this loop form issues fastest; see the issuer)
+        for (int kb = 0; kb < nkb && ok; ++kb) {
+          const int64_t t = kb0 + kb;
+          for (int m = 0; m < nqt; ++m) {
+            if (!mbar_wait_lim(&empty_a[stage], phase ^ 1, abort_flag, spin)) {
+              ok = false;
+              break;
+            }
+            mbar_expect_tx(&full_a[stage], F8_ATILE);
+            uint8_t *dst = aring + stage * F8_ATILE;
+            const int q = (qt0 + m) * F8_BM;
+            if (prm.mmajor) {
+              tma_load_2d(dst, &tmap, &full_a[stage], q, (int)(t * F8_BK));
+            } else {
+              const int s = (int)(t / prm.pblocks);
+              const int p0 = (int)((t % prm.pblocks) * F8_BK);
+              tma_load_3d(dst, &tmap, &full_a[stage], p0, q, s);
+            }
+            ++issued[stage];
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
-          mbar_expect_tx(&full_a[stage], F8_ATILE);
-          uint8_t *dst = aring + stage * F8_ATILE;
+        }
+      }
+      for (int g0 = 0; G > 1 && g0 < nkb && ok; g0 += G) {
+        const int gn = min(G, nkb - g0);
+        const int64_t tg = kb0 + g0;
+        int sg, pg = 0;
+        if (prm.mmajor) {
+          sg = (int)(tg * F8_BK);
+        } else {
+          sg = (int)(tg / prm.pblocks);
+          pg = (int)((tg - (int64_t)sg * prm.pblocks) * F8_BK);
+        }
+        for (int m = 0; m < nqt && ok; ++m) {
           const int q = (qt0 + m) * F8_BM;
-          if (prm.mmajor) {
-            tma_load_2d(dst, &tmap, &full_a[stage], q, (int)(t * F8_BK));
-          } else {
-            const int s = (int)(t / prm.pblocks);
-            const int p0 = (int)((t % prm.pblocks) * F8_BK);
-            tma_load_3d(dst, &tmap, &full_a[stage], p0, q, s);
-          }
-          ++issued[stage];
-          if (++stage == STAGES) {
-            stage = 0;
-            phase ^= 1;
+          int s = sg, p = pg;
+          for (int j = 0; j < gn; ++j) {
+            if (!mbar_wait_lim(&empty_a[stage], phase ^ 1, abort_flag, spin)) {
+              ok = false;
+              break;
+            }
+            mbar_expect_tx(&full_a[stage], F8_ATILE);
+            uint8_t *dst = aring + stage * F8_ATILE;
+            if (prm.mmajor) {
+              tma_load_2d(dst, &tmap, &full_a[stage], q, s);
+              s += F8_BK;
+            } else {
+              tma_load_3d(dst, &tmap, &full_a[stage], p, q, s);
+              p += F8_BK;
+              if (p == pend) {
+                p = 0;
+                ++s;
+              }
+            }
+            ++issued[stage];
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
         }
       }
@@ -403,38 +449,83 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
       int stage = 0, kst = 0;
       uint32_t phase = 0, kphase = 0;
       bool ok = true;
-      for (int kb = 0; kb < nkb && ok; ++kb) {
-        if (!mbar_wait_lim(&full_k[kst], kphase, abort_flag, spin)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t kaddr = smem_u32(kring + kst * KTILE);
-        for (int m = 0; m < nqt; ++m) {
-          if (!mbar_wait_lim(&full_a[stage], phase, abort_flag, spin)) {
+      // descriptors: a constant high word and the start address >> 4, stepped per K = 32 codes
+      // (32 bytes along a K-major row, or 32 rows of 128 bytes of the MN-major tile: 4 groups
+      // of 8 rows, 1024 bytes apart)
+      const uint64_t a_hi = prm.mmajor ? smem_desc_sw128_hi(8192, 1024) : smem_desc_sw128_hi(16, 1024);
+      const uint64_t b_hi = smem_desc_sw128_hi(16, 1024);
+      const uint32_t a_step = prm.mmajor ? (4096u >> 4) : (32u >> 4);
+      const uint32_t a_lo0 = smem_u32(aring) >> 4, k_lo0 = smem_u32(kring) >> 4;
+      if (G == 1) {
+        // one K-block at a time, descriptors built next to each MMA: measured faster than the
+        // group loop below with G = 1 (the issuing thread is the busiest role of the kernel)
+        for (int kb = 0; kb < nkb && ok; ++kb) {
+          if (!mbar_wait_lim(&full_k[kst], kphase, abort_flag, spin)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t aaddr = smem_u32(aring + stage * F8_ATILE);
+          const uint32_t kaddr = smem_u32(kring + kst * KTILE);
+          for (int m = 0; m < nqt; ++m) {
+            if (!mbar_wait_lim(&full_a[stage], phase, abort_flag, spin)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t aaddr = smem_u32(aring + stage * F8_ATILE);
 #pragma unroll
-          for (int kk = 0; kk < F8_BK / 32; ++kk) {
-            // K = 32 codes per MMA: 32 bytes along a K-major row, or 32 rows of 128 bytes of
-            // the MN-major tile (4 groups of 8 rows, 1024 bytes apart)
-            const uint64_t ad = prm.mmajor ? smem_desc_sw128(aaddr + kk * 4096, 8192, 1024)
-                                           : smem_desc_sw128(aaddr + kk * 32, 16, 1024);
-            const uint64_t bd = smem_desc_sw128(kaddr + kk * 32, 16, 1024);
-            umma_f8(tmem_base + (uint32_t)(m * N), ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            for (int kk = 0; kk < F8_BK / 32; ++kk) {
+              const uint64_t ad = prm.mmajor ? smem_desc_sw128(aaddr + kk * 4096, 8192, 1024)
+                                             : smem_desc_sw128(aaddr + kk * 32, 16, 1024);
+              const uint64_t bd = smem_desc_sw128(kaddr + kk * 32, 16, 1024);
+              umma_f8(tmem_base + (uint32_t)(m * N), ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            }
+            umma_commit(&empty_a[stage]);
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
-          umma_commit(&empty_a[stage]);
-          if (++stage == STAGES) {
-            stage = 0;
-            phase ^= 1;
+          if (!ok) break;
+          umma_commit(&empty_k[kst]);
+          if (++kst == KSTAGES) {
+            kst = 0;
+            kphase ^= 1;
+          }
+        }
+      }
+      // a group's Khatri-Rao tiles sit in ring slots kst .. kst + gn - 1: the ring holds a
+      // whole number of groups, so a group never wraps around its end
+      for (int g0 = 0; G > 1 && g0 < nkb && ok; g0 += G) {
+        const int gn = min(G, nkb - g0);
+        for (int j = 0; j < gn && ok; ++j) ok = mbar_wait_lim(&full_k[kst + j], kphase, abort_flag, spin);
+        if (!ok) break;
+        tc_fence_after();
+        for (int m = 0; m < nqt && ok; ++m) {
+          const uint32_t d_tmem = tmem_base + (uint32_t)(m * N);
+          for (int j = 0; j < gn; ++j) {
+            if (!mbar_wait_lim(&full_a[stage], phase, abort_flag, spin)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint64_t ad = a_hi | (uint64_t)(a_lo0 + (uint32_t)stage * (F8_ATILE >> 4));
+            const uint64_t bd = b_hi | (uint64_t)(k_lo0 + (uint32_t)(kst + j) * (uint32_t)(KTILE >> 4));
+            umma_f8(d_tmem, ad, bd, idesc, (g0 | j) != 0 ? 1u : 0u);
+#pragma unroll
+            for (int kk = 1; kk < F8_BK / 32; ++kk)
+              umma_f8(d_tmem, ad + kk * a_step, bd + kk * (32u >> 4), idesc, 1u);
+            umma_commit(&empty_a[stage]);
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
         }
         if (!ok) break;
-        umma_commit(&empty_k[kst]);
-        if (++kst == KSTAGES) {
+        for (int j = 0; j < gn; ++j) umma_commit(&empty_k[kst + j]);
+        kst += G;
+        if (kst == KSTAGES) {
           kst = 0;
           kphase ^= 1;
         }
@@ -454,6 +545,9 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
     const bool drains = warp < 6;               // warps 2..5 cover the four TMEM lane quarters
     int kst = 0;
     uint32_t kphase = 0;
+    // slab and p-block of K-block kb0 + kb (modes n >= 1), stepped without dividing
+    int64_t sl = kb0 / prm.pblocks;
+    int pb = (int)(kb0 - sl * prm.pblocks);
     for (int kb = 0; kb < nkb; ++kb) {
       if (!mbar_wait_lim(&empty_k[kst], kphase ^ 1, abort_flag, spin)) {
         *abort_flag = 1;
@@ -469,10 +563,9 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
         valid = s < prm.S;
         lin_a = (uint32_t)s;
       } else {
-        const int64_t s = t / prm.pblocks;
-        const int64_t p = (t % prm.pblocks) * F8_BK + k;
+        const int64_t p = (int64_t)pb * F8_BK + k;
         valid = p < prm.P;
-        lin_a = (uint32_t)s;
+        lin_a = (uint32_t)sl;
         lin_b = (uint32_t)p;
       }
       const float row_sc = (valid && !prm.slab_in_q) ? __ldg(prm.slab_scale + (int64_t)lin_a / prm.slab_div) : 1.0f;
@@ -499,6 +592,10 @@ mttkrp_f8_kernel(const __grid_constant__ CUtensorMap tmap, const F8Params prm) {
       }
       fence_async_smem();
       mbar_arrive(&full_k[kst]);
+      if (++pb == prm.pblocks) {
+        pb = 0;
+        ++sl;
+      }
       if (++kst == KSTAGES) {
         kst = 0;
         kphase ^= 1;
@@ -630,11 +727,17 @@ int f8_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &
   nsplit = std::min<int64_t>(nsplit, prm.kblocks_total);
   prm.kblocks_per_split = (prm.kblocks_total + nsplit - 1) / nsplit;
   nsplit = (prm.kblocks_total + prm.kblocks_per_split - 1) / prm.kblocks_per_split;
-  // the rings: 8 X stages and 4 Khatri-Rao stages while they fit in one CTA's shared memory
-  prm.stages = F8_MAX_STAGES;
+  // The rings take at most the shared memory that leaves room on the SM for the eigenvalue-
+  // bound kernel beside it: an X ring of up to 6 stages and a Khatri-Rao ring of two groups
+  // (a mode-0 K-block is one contiguous run of X: G = 1 there)
+  const size_t budget = ctx->smem_beside_eigen;
+  const int G = mmajor ? 1 : F8_GROUP;
+  prm.group = G;
   prm.kstages = F8_MAX_KSTAGES;
-  while (f8_smem_bytes(prm.N, prm.stages, prm.kstages) > ctx->smem_optin && prm.kstages > 2) --prm.kstages;
-  while (f8_smem_bytes(prm.N, prm.stages, prm.kstages) > ctx->smem_optin && prm.stages > 3) --prm.stages;
+  prm.stages = F8_MAX_STAGES;
+  while (f8_smem_bytes(prm.N, prm.stages, prm.kstages) > budget && prm.stages > 3) --prm.stages;
+  while (f8_smem_bytes(prm.N, prm.stages, prm.kstages) > ctx->smem_optin && prm.kstages > 2 && G == 1)
+    --prm.kstages;
   const size_t smem = f8_smem_bytes(prm.N, prm.stages, prm.kstages);
   if (smem > ctx->smem_optin) return set_error(PTG_ERR_UNSUPPORTED, "FP8 MTTKRP: shared memory");
 

@@ -64,6 +64,9 @@ struct ptg_ctx {
   int sm_count = 0;
   int cc_major = 0, cc_minor = 0;
   size_t smem_optin = 0;
+  // dynamic shared memory a one-CTA-per-SM contraction kernel may take so that the FP64
+  // eigenvalue-bound kernel, launched beside it on a side stream, still fits on its SM
+  size_t smem_beside_eigen = 0;
   cudaStream_t stream = nullptr;      // main stream (own or caller's)
   cudaStream_t own_stream = nullptr;
   cudaStream_t side = nullptr;        // concurrent small kernels (FP64 eigenbounds)
@@ -346,6 +349,8 @@ struct CostScratch {
 constexpr int kCostPartials = 64;
 int launch_cost_terms(const float *M, const float *A_last, int64_t I_last, const float *const *grams,
                       int order, int R, double *out2, CostScratch scratch, cudaStream_t stream);
+// static shared memory of the FP64 eigenvalue-bound kernel (one CTA)
+size_t eigen_kernel_smem();
 // *out = sum over (r1, r2) of prod_k (A_k^T A_k)[r1][r2], the Grams accumulated in FP64 from the
 // factors (part: gram_term_fp64_scratch_doubles(order, R) doubles of scratch)
 size_t gram_term_fp64_scratch_doubles(int order, int R);

@@ -4,7 +4,10 @@
 // [P, Q, S], out[q, r] = sum_{p,s} X[p,q,s] KRb[p,r] KRa[s,r].  One CTA per SM, warp
 // specialised:
 //   warp 0      TMA producer: 128 x 64 BF16 tiles of X into a ring of shared-memory stages
-//               (128-byte swizzle; K-major for modes n >= 1, MN-major for mode 0);
+//               (128-byte swizzle; K-major for modes n >= 1, MN-major for mode 0).  K-blocks
+//               go in groups of G consecutive ones: within a group the q-tiles are the outer
+//               loop, so each row of X is read as one run of G x 128 bytes (a mode-0 K-block
+//               is already one contiguous run; there G = 1);
 //   warp 1      allocates TMEM and issues tcgen05.mma (M=128, N=R padded to 16, K=16) from
 //               one elected lane; each q-tile of the CTA accumulates in its own TMEM columns;
 //   warps 2..9  build the R x 64 Khatri-Rao tile of every K-block in shared memory (BF16,
@@ -29,8 +32,9 @@ using namespace tc;
 
 constexpr int TC_BM = 128;         // q rows per tile (MMA M)
 constexpr int TC_BK = 64;          // contraction elements per K-block (one 128-byte row)
-constexpr int TC_STAGES = 8;       // X tile ring
-constexpr int TC_KSTAGES = 4;      // Khatri-Rao tile ring
+constexpr int TC_MAX_STAGES = 8;   // X tile ring (fewer when the shared-memory budget is short)
+constexpr int TC_GROUP = 2;        // K-blocks per group, modes n >= 1 (measured: 2 beats 1 and 4)
+constexpr int TC_MAX_KSTAGES = 4;  // Khatri-Rao tile ring: two groups
 constexpr int TC_THREADS = 320;    // producer, MMA issuer, 8 Khatri-Rao builder warps
 constexpr int TC_BUILDERS = 256;
 constexpr int TC_ATILE = TC_BM * TC_BK * 2;   // 16 KB
@@ -42,6 +46,9 @@ struct TcParams {
   int N;          // MMA N: rank padded to a multiple of 16
   int R;
   int mmajor;
+  int stages;      // X ring stages
+  int group;       // G: K-blocks per group
+  int kstages;     // Khatri-Rao ring stages (a multiple of G, >= 2 G)
   uint32_t tmem_cols;
   uint32_t spin;   // poll limit of every bounded wait
   int vec4;        // factor rows are read as float4 (R % 4 == 0, 16-byte aligned)
@@ -60,11 +67,12 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
   const int N = prm.N;
   const int KTILE = N * 128;                       // R_pad rows of 128 bytes
   uint8_t *aring = base;
-  uint8_t *kring = aring + TC_STAGES * TC_ATILE;
-  uint64_t *bars = (uint64_t *)(kring + TC_KSTAGES * KTILE);
-  uint64_t *full_a = bars, *empty_a = bars + TC_STAGES;
-  uint64_t *full_k = empty_a + TC_STAGES, *empty_k = full_k + TC_KSTAGES;
-  uint64_t *done = empty_k + TC_KSTAGES;
+  const int STAGES = prm.stages, KSTAGES = prm.kstages, G = prm.group;
+  uint8_t *kring = aring + STAGES * TC_ATILE;
+  uint64_t *bars = (uint64_t *)(kring + KSTAGES * KTILE);
+  uint64_t *full_a = bars, *empty_a = bars + TC_MAX_STAGES;
+  uint64_t *full_k = empty_a + TC_MAX_STAGES, *empty_k = full_k + TC_MAX_KSTAGES;
+  uint64_t *done = empty_k + TC_MAX_KSTAGES;
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
   volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
@@ -77,11 +85,11 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
   const int nkb = kb1 > kb0 ? (int)(kb1 - kb0) : 0;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < TC_STAGES; ++i) {
+    for (int i = 0; i < STAGES; ++i) {
       mbar_init(&full_a[i], 1);
       mbar_init(&empty_a[i], 1);
     }
-    for (int i = 0; i < TC_KSTAGES; ++i) {
+    for (int i = 0; i < KSTAGES; ++i) {
       mbar_init(&full_k[i], TC_BUILDERS);
       mbar_init(&empty_k[i], 1);
     }
@@ -109,31 +117,76 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
     if (lane == 0 && nkb > 0) {
       int stage = 0;
       uint32_t phase = 0;
-      int issued[TC_STAGES] = {0};   // loads issued into each stage
+      int issued[TC_MAX_STAGES] = {0};   // loads issued into each stage
       bool ok = true;
-      for (int kb = 0; kb < nkb && ok; ++kb) {
-        const int64_t t = kb0 + kb;
-        for (int m = 0; m < nqt; ++m) {
-          if (!mbar_wait_lim(&empty_a[stage], phase ^ 1, abort_flag, prm.spin)) {
-            ok = false;
-            break;
+      // K-block t covers s in [t BK, t BK + BK) (mode 0), else slab t / pblocks, p from
+      // (t % pblocks) BK; the coordinates step along a group without dividing
+      const int pend = (int)(prm.pblocks * TC_BK);
+      if (G == 1) {   // one K-block at a time (this loop form issues fastest; see the issuer)
+        for (int kb = 0; kb < nkb && ok; ++kb) {
+          const int64_t t = kb0 + kb;
+          for (int m = 0; m < nqt; ++m) {
+            if (!mbar_wait_lim(&empty_a[stage], phase ^ 1, abort_flag, prm.spin)) {
+              ok = false;
+              break;
+            }
+            mbar_expect_tx(&full_a[stage], TC_ATILE);
+            uint8_t *dst = aring + stage * TC_ATILE;
+            const int q = (qt0 + m) * TC_BM;
+            if (prm.mmajor) {
+              const int s0 = (int)(t * TC_BK);
+              tma_load_2d(dst, &tmap, &full_a[stage], q, s0);
+              tma_load_2d(dst + TC_ATILE / 2, &tmap, &full_a[stage], q + 64, s0);
+            } else {
+              const int s = (int)(t / prm.pblocks);
+              const int p0 = (int)((t % prm.pblocks) * TC_BK);
+              tma_load_3d(dst, &tmap, &full_a[stage], p0, q, s);
+            }
+            ++issued[stage];
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
-          mbar_expect_tx(&full_a[stage], TC_ATILE);
-          uint8_t *dst = aring + stage * TC_ATILE;
+        }
+      }
+      for (int g0 = 0; G > 1 && g0 < nkb && ok; g0 += G) {
+        const int gn = min(G, nkb - g0);
+        const int64_t tg = kb0 + g0;
+        int sg, pg = 0;
+        if (prm.mmajor) {
+          sg = (int)(tg * TC_BK);
+        } else {
+          sg = (int)(tg / prm.pblocks);
+          pg = (int)((tg - (int64_t)sg * prm.pblocks) * TC_BK);
+        }
+        for (int m = 0; m < nqt && ok; ++m) {
           const int q = (qt0 + m) * TC_BM;
-          if (prm.mmajor) {
-            const int s0 = (int)(t * TC_BK);
-            tma_load_2d(dst, &tmap, &full_a[stage], q, s0);
-            tma_load_2d(dst + TC_ATILE / 2, &tmap, &full_a[stage], q + 64, s0);
-          } else {
-            const int s = (int)(t / prm.pblocks);
-            const int p0 = (int)((t % prm.pblocks) * TC_BK);
-            tma_load_3d(dst, &tmap, &full_a[stage], p0, q, s);
-          }
-          ++issued[stage];
-          if (++stage == TC_STAGES) {
-            stage = 0;
-            phase ^= 1;
+          int s = sg, p = pg;
+          for (int j = 0; j < gn; ++j) {
+            if (!mbar_wait_lim(&empty_a[stage], phase ^ 1, abort_flag, prm.spin)) {
+              ok = false;
+              break;
+            }
+            mbar_expect_tx(&full_a[stage], TC_ATILE);
+            uint8_t *dst = aring + stage * TC_ATILE;
+            if (prm.mmajor) {
+              tma_load_2d(dst, &tmap, &full_a[stage], q, s);
+              tma_load_2d(dst + TC_ATILE / 2, &tmap, &full_a[stage], q + 64, s);
+              s += TC_BK;
+            } else {
+              tma_load_3d(dst, &tmap, &full_a[stage], p, q, s);
+              p += TC_BK;
+              if (p == pend) {
+                p = 0;
+                ++s;
+              }
+            }
+            ++issued[stage];
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
         }
       }
@@ -144,7 +197,7 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
       // a stage holds at most one load in flight (the next one waits for its release), the
       // last one issued into it: wait for each so no copy lands after the CTA has exited
       // (loads that were consumed completed long ago and return at once)
-      for (int s = 0; s < TC_STAGES; ++s)
+      for (int s = 0; s < STAGES; ++s)
         if (issued[s] > 0) mbar_wait_bounded(&full_a[s], (uint32_t)((issued[s] - 1) & 1));
     }
   } else if (warp == 1) {
@@ -153,36 +206,82 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
       int stage = 0, kst = 0;
       uint32_t phase = 0, kphase = 0;
       bool ok = true;
-      for (int kb = 0; kb < nkb && ok; ++kb) {
-        if (!mbar_wait_lim(&full_k[kst], kphase, abort_flag, prm.spin)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t kaddr = smem_u32(kring + kst * KTILE);
-        for (int m = 0; m < nqt; ++m) {
-          if (!mbar_wait_lim(&full_a[stage], phase, abort_flag, prm.spin)) {
+      // descriptors: a constant high word and the start address >> 4, stepped per K = 16
+      const uint64_t a_hi = prm.mmajor ? smem_desc_sw128_hi(TC_ATILE / 2, 1024) : smem_desc_sw128_hi(16, 1024);
+      const uint64_t b_hi = smem_desc_sw128_hi(16, 1024);
+      const uint32_t a_step = prm.mmajor ? (2048u >> 4) : (32u >> 4);
+      const uint32_t a_lo0 = smem_u32(aring) >> 4, k_lo0 = smem_u32(kring) >> 4;
+      if (G == 1) {
+        // one K-block at a time, descriptors built next to each MMA: measured faster than the
+        // group loop below with G = 1 (the issuing thread is the busiest role of the kernel)
+        for (int kb = 0; kb < nkb && ok; ++kb) {
+          if (!mbar_wait_lim(&full_k[kst], kphase, abort_flag, prm.spin)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t aaddr = smem_u32(aring + stage * TC_ATILE);
+          const uint32_t kaddr = smem_u32(kring + kst * KTILE);
+          for (int m = 0; m < nqt; ++m) {
+            if (!mbar_wait_lim(&full_a[stage], phase, abort_flag, prm.spin)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t aaddr = smem_u32(aring + stage * TC_ATILE);
 #pragma unroll
-          for (int kk = 0; kk < TC_BK / 16; ++kk) {
-            const uint64_t ad = prm.mmajor ? smem_desc_sw128(aaddr + kk * 2048, TC_ATILE / 2, 1024)
-                                           : smem_desc_sw128(aaddr + kk * 32, 16, 1024);
-            const uint64_t bd = smem_desc_sw128(kaddr + kk * 32, 16, 1024);
-            umma_bf16(tmem_base + (uint32_t)(m * N), ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            for (int kk = 0; kk < TC_BK / 16; ++kk) {
+              const uint64_t ad = prm.mmajor ? smem_desc_sw128(aaddr + kk * 2048, TC_ATILE / 2, 1024)
+                                             : smem_desc_sw128(aaddr + kk * 32, 16, 1024);
+              const uint64_t bd = smem_desc_sw128(kaddr + kk * 32, 16, 1024);
+              umma_bf16(tmem_base + (uint32_t)(m * N), ad, bd, idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            }
+            umma_commit(&empty_a[stage]);
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
-          umma_commit(&empty_a[stage]);
-          if (++stage == TC_STAGES) {
-            stage = 0;
-            phase ^= 1;
+          if (!ok) break;
+          umma_commit(&empty_k[kst]);
+          if (++kst == KSTAGES) {
+            kst = 0;
+            kphase ^= 1;
+          }
+        }
+      }
+      // a group's Khatri-Rao tiles sit in ring slots kst .. kst + gn - 1: the ring holds a
+      // whole number of groups, so a group never wraps around its end
+      for (int g0 = 0; G > 1 && g0 < nkb && ok; g0 += G) {
+        const int gn = min(G, nkb - g0);
+        for (int j = 0; j < gn && ok; ++j)
+          ok = mbar_wait_lim(&full_k[kst + j], kphase, abort_flag, prm.spin);
+        if (!ok) break;
+        tc_fence_after();
+        for (int m = 0; m < nqt && ok; ++m) {
+          const uint32_t d_tmem = tmem_base + (uint32_t)(m * N);
+          for (int j = 0; j < gn; ++j) {
+            if (!mbar_wait_lim(&full_a[stage], phase, abort_flag, prm.spin)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint64_t ad = a_hi | (uint64_t)(a_lo0 + (uint32_t)stage * (TC_ATILE >> 4));
+            const uint64_t bd = b_hi | (uint64_t)(k_lo0 + (uint32_t)(kst + j) * (uint32_t)(KTILE >> 4));
+            umma_bf16(d_tmem, ad, bd, idesc, (g0 | j) != 0 ? 1u : 0u);
+#pragma unroll
+            for (int kk = 1; kk < TC_BK / 16; ++kk)
+              umma_bf16(d_tmem, ad + kk * a_step, bd + kk * (32u >> 4), idesc, 1u);
+            umma_commit(&empty_a[stage]);
+            if (++stage == STAGES) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
         }
         if (!ok) break;
-        umma_commit(&empty_k[kst]);
-        if (++kst == TC_KSTAGES) {
+        for (int j = 0; j < gn; ++j) umma_commit(&empty_k[kst + j]);
+        kst += G;
+        if (kst == KSTAGES) {
           kst = 0;
           kphase ^= 1;
         }
@@ -202,6 +301,9 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
     const bool drains = warp < 6;            // warps 2..5 cover the four TMEM lane quarters
     int kst = 0;
     uint32_t kphase = 0;
+    // slab and p-block of K-block kb0 + kb (modes n >= 1), stepped without dividing
+    int64_t sl = kb0 / prm.pblocks;
+    int pb = (int)(kb0 - sl * prm.pblocks);
     for (int kb = 0; kb < nkb; ++kb) {
       if (!mbar_wait_lim(&empty_k[kst], kphase ^ 1, abort_flag, prm.spin)) {
         *abort_flag = 1;
@@ -218,10 +320,9 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
         valid = s < prm.S;
         lin_a = (uint32_t)s;
       } else {
-        const int64_t s = t / prm.pblocks;
-        const int64_t p = (t % prm.pblocks) * TC_BK + k;
+        const int64_t p = (int64_t)pb * TC_BK + k;
         valid = p < prm.P;
-        lin_a = (uint32_t)s;
+        lin_a = (uint32_t)sl;
         lin_b = (uint32_t)p;
       }
       // the thread's 8-column chunks, the loads of a chunk's factor rows issued together
@@ -243,7 +344,11 @@ mttkrp_tc_kernel(const __grid_constant__ CUtensorMap tmap, const TcParams prm) {
       }
       fence_async_smem();
       mbar_arrive(&full_k[kst]);
-      if (++kst == TC_KSTAGES) {
+      if (++pb == prm.pblocks) {
+        pb = 0;
+        ++sl;
+      }
+      if (++kst == KSTAGES) {
         kst = 0;
         kphase ^= 1;
       }
@@ -293,9 +398,9 @@ __global__ void tc_reduce_kernel(const float *__restrict__ partial, int nsplit, 
   }
 }
 
-size_t tc_smem_bytes(int N) {
-  return 1024 /*alignment slack*/ + (size_t)TC_STAGES * TC_ATILE + (size_t)TC_KSTAGES * N * 128 +
-         sizeof(uint64_t) * (2 * TC_STAGES + 2 * TC_KSTAGES + 1) + 16;
+size_t tc_smem_bytes(int N, int stages, int kstages) {
+  return 1024 /*alignment slack*/ + (size_t)stages * TC_ATILE + (size_t)kstages * N * 128 +
+         sizeof(uint64_t) * (2 * TC_MAX_STAGES + 2 * TC_MAX_KSTAGES + 1) + 16;
 }
 
 }  // namespace
@@ -385,13 +490,24 @@ int tc_contraction_launch(ptg_ctx *ctx, const ptg_tensor *t, const Contraction &
   prm.partial = reinterpret_cast<float *>(ctx->scratch.ptr);
   prm.err = ctx->dev_err;
   prm.skip = c.skip;
-  const size_t smem = tc_smem_bytes(prm.N);
-  PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // The rings take at most the shared memory that leaves room on the SM for the eigenvalue-
+  // bound kernel beside it: an X ring of up to 8 stages (more measured no faster) and a
+  // Khatri-Rao ring of two groups
+  const size_t budget = ctx->smem_beside_eigen;
+  prm.group = mmajor ? 1 : TC_GROUP;
+  prm.kstages = TC_MAX_KSTAGES;
+  int stages = TC_MAX_STAGES;
+  while (stages > 4 && tc_smem_bytes(prm.N, stages, prm.kstages) > budget) --stages;
+  prm.stages = stages;
+  const size_t smem = tc_smem_bytes(prm.N, prm.stages, prm.kstages);
+  if (smem > ctx->smem_optin) return set_error(PTG_ERR_UNSUPPORTED, "tcgen05 MTTKRP: shared memory");
+  auto kern = mttkrp_tc_kernel;
+  PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // the largest carveout, which the eigenvalue-bound kernel beside it asks for too
-  PTG_CUDA(cudaFuncSetAttribute(mttkrp_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+  PTG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                                 cudaSharedmemCarveoutMaxShared));
   dim3 grid((unsigned)qgroups, (unsigned)nsplit);
-  mttkrp_tc_kernel<<<grid, TC_THREADS, smem, stream>>>(map, prm);
+  kern<<<grid, TC_THREADS, smem, stream>>>(map, prm);
   PTG_CUDA(cudaGetLastError());
   const int64_t n = c.q_write * R;
   const int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ctx->sm_count * 8);

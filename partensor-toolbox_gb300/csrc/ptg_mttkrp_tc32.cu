@@ -40,7 +40,6 @@ using namespace tc;
 
 constexpr int T3_BM = 128;                     // q rows per tile (MMA M)
 constexpr int T3_BK = 32;                      // contraction elements per K-block (128-byte rows)
-constexpr int T3_XSTAGES = 8;                  // TMA staging ring (FP32 tiles as loaded)
 constexpr int T3_SSTAGES = 2;                  // split ring: hi and lo K-major tiles
 constexpr int T3_KSTAGES = 2;                  // Khatri-Rao ring: [hi rows; lo rows]
 constexpr int T3_TILE = T3_BM * T3_BK * 4;     // 16 KB
@@ -54,6 +53,9 @@ template <int N>
 struct T3Shape {
   static constexpr int MT = 128 / N > 8 ? 8 : 128 / N;
   static constexpr int HALF = N / 2;
+  // staging stages: as many as leave room on the SM for the eigenvalue-bound kernel launched
+  // beside this one (its 39 KB of shared memory; 228 KB per SM)
+  static constexpr int XST = N <= 16 ? 7 : N <= 48 ? 6 : 5;
 };
 
 // Chain c's accumulator, columns [col0, col0 + HALF) of both halves, added into the sums of
@@ -129,15 +131,18 @@ __device__ __forceinline__ void fail_timeout(volatile int *abort_flag, int *err)
   atomicExch(err, PTG_ERR_TIMEOUT);
 }
 
+// At most 160 registers a thread: 320 x 160 leaves 14,336 of the SM's 65,536 for the
+// eigenvalue-bound kernel's 256 threads beside it.
 template <int N>
-__global__ void __launch_bounds__(T3_THREADS, 1)
+__global__ void __maxnreg__(160)
 mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm) {
   constexpr int MT = T3Shape<N>::MT;
+  constexpr int T3_XSTAGES = T3Shape<N>::XST;
   if (prm.skip && *prm.skip) return;   // before any barrier or TMEM allocation
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int KTILE = 2 * N * 128;                       // [hi rows 0..N-1; lo rows N..2N-1]
-  uint8_t *xring = base;                                   // [8] staging tiles
+  uint8_t *xring = base;                                   // [T3_XSTAGES] staging tiles
   uint8_t *sring = xring + T3_XSTAGES * T3_TILE;           // [2]{hi, lo}
   uint8_t *kring = sring + T3_SSTAGES * 2 * T3_TILE;       // [2] Khatri-Rao tiles
   uint64_t *bars = (uint64_t *)(kring + T3_KSTAGES * KTILE);
@@ -189,7 +194,7 @@ mttkrp_tc32_kernel(const __grid_constant__ CUtensorMap tmap, const T3Params prm)
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
-  uint32_t issued[T3_XSTAGES] = {0, 0, 0, 0, 0, 0, 0, 0};   // TMA loads per stage (producer lane)
+  uint32_t issued[T3_XSTAGES] = {};   // TMA loads per stage (producer lane)
   if (warp == 0) {
     // ---------------- TMA producer ----------------
     if (lane == 0 && nkb > 0) {
@@ -493,9 +498,11 @@ __global__ void tc32_reduce_kernel(const float *__restrict__ partial, int nsplit
 }
 
 size_t tc32_smem_bytes(int N) {
-  return 1024 /*alignment slack*/ + (size_t)T3_XSTAGES * T3_TILE + (size_t)T3_SSTAGES * 2 * T3_TILE +
+  const int xst = N == 16 ? T3Shape<16>::XST : N == 32 ? T3Shape<32>::XST : N == 48 ? T3Shape<48>::XST
+                                                                                 : T3Shape<64>::XST;
+  return 1024 /*alignment slack*/ + (size_t)xst * T3_TILE + (size_t)T3_SSTAGES * 2 * T3_TILE +
          (size_t)T3_KSTAGES * 2 * N * 128 +
-         sizeof(uint64_t) * (2 * T3_XSTAGES + 2 * T3_SSTAGES + 2 * T3_KSTAGES + 4 + 1) + 16;
+         sizeof(uint64_t) * (2 * xst + 2 * T3_SSTAGES + 2 * T3_KSTAGES + 4 + 1) + 16;
 }
 
 }  // namespace

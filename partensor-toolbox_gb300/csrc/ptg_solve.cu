@@ -564,6 +564,15 @@ __global__ void sum_rr_kernel(const float *__restrict__ part, int nb, int RR, fl
 
 }  // namespace
 
+size_t eigen_kernel_smem() {
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, eigen_bounds_kernel) != cudaSuccess) {
+    cudaGetLastError();
+    return 48 * 1024;
+  }
+  return fa.sharedSizeBytes;
+}
+
 int launch_eigen_bounds(const float *const *grams, int order, int mode, int R, NnlsParams *out,
                         cudaStream_t stream, bool beside_tc) {
   if (R > kMaxR) return set_error(PTG_ERR_UNSUPPORTED, "rank > 64 is not supported by the NNLS path");

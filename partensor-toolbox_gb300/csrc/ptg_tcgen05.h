@@ -97,6 +97,14 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr, uint32_t lbo,
   return d;
 }
 
+// The same descriptor without its start address: the start field (bits 0-13, address >> 4)
+// is ORed in by the caller, and stepping the start by b bytes adds b >> 4 (no carry: shared
+// addresses are below 2^18).
+__device__ __forceinline__ uint64_t smem_desc_sw128_hi(uint32_t lbo, uint32_t sbo) {
+  return ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46) |
+         ((uint64_t)2 << 61);
+}
+
 __device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                           uint32_t accumulate) {
   asm volatile(
