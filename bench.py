@@ -347,12 +347,12 @@ def run_ours(args):
                 "ms_per_launch": per_launch_ms, "bytes_per_launch": bytes_per_launch, "traffic_source": note}
 
     # DRAM bytes per launch from ncu captures at 640^3 (mode 1), scaled by the entries of this
-    # workload: BF16 read 530.58 MB + write 3.66 MB
+    # workload: BF16 read 530.79 MB + write 3.38 MB, FP8 read 272.64 MB + write 3.72 MB
     scale = float(np.prod(dims)) / 640 ** 3
     roof_b = roofline(kst, "mttkrp_tc_kernel + tc_reduce_kernel (tcgen05 kind::f16, BF16 storage)",
-                      (530.58e6 + 3.66e6) * scale, "ncu capture at 640^3 scaled by entries (profiles/)")
+                      (530.79e6 + 3.38e6) * scale, "ncu capture at 640^3 scaled by entries (profiles/)")
     roof_8 = roofline(kst8, "f8_colscale_kernel + mttkrp_f8_kernel + f8_reduce_kernel (tcgen05 kind::f8f6f4)",
-                      None, "no ncu capture of this build yet")
+                      (272.64e6 + 3.72e6) * scale, "ncu capture at 640^3 scaled by entries (profiles/)")
 
     def parity(st):
         tr = [t["rel"] for t in st.trace][: st.ao_iter]
