@@ -40,6 +40,7 @@ eigen_bounds_kernel(GramPtrs gp, int order, int mode, int R, NnlsParams *out) {
 // without spills: 1000^3 BF16 solve 30.4 vs 30.8 ms.
 constexpr int kNnlsWarpsLarge = 16;
 constexpr int kNnlsWindowMax = 8;
+constexpr int kNnlsMaxCluster = 16;   // the largest cluster the launch asks for
 
 struct NnlsArgs {
   const float *M;        // [I][R]
@@ -374,14 +375,20 @@ __global__ void __launch_bounds__(W * 32, 1) nnls_cluster_kernel(const NnlsArgs 
     colsum[c] = s;
   }
   cluster.sync();
-  if (tid == 0) {
+  if (warp == 0) {   // a lane per column; the CTAs' sums loaded together, added in rank order
     float mincol = INFINITY;
-    for (int c = 0; c < R; ++c) {
+    for (int c = lane; c < R; c += 32) {
+      float v[kNnlsMaxCluster];
+#pragma unroll
+      for (int r2 = 0; r2 < kNnlsMaxCluster; ++r2) v[r2] = r2 < CS ? cluster.map_shared_rank(colsum, r2)[c] : 0.f;
       float s = 0.f;
-      for (int r2 = 0; r2 < CS; ++r2) s += cluster.map_shared_rank(colsum, r2)[c];
+#pragma unroll
+      for (int r2 = 0; r2 < kNnlsMaxCluster; ++r2)
+        if (r2 < CS) s += v[r2];
       mincol = fminf(mincol, s);
     }
-    flags[0] = (mincol == 0.0f) ? 1 : 0;
+    for (int o = 16; o > 0; o >>= 1) mincol = fminf(mincol, __shfl_xor_sync(0xffffffffu, mincol, o));
+    if (lane == 0) flags[0] = (mincol == 0.0f) ? 1 : 0;
   }
   __syncthreads();
   const bool repair = flags[0] != 0;
@@ -437,8 +444,13 @@ __global__ void __launch_bounds__(W * 32, 1) nnls_cluster_kernel(const NnlsArgs 
   cluster.sync();
   if (rank == 0) {
     for (int idx = tid; idx < R * R; idx += blockDim.x) {
+      float v[kNnlsMaxCluster];   // the CTAs' partials loaded together, added in rank order
+#pragma unroll
+      for (int r2 = 0; r2 < kNnlsMaxCluster; ++r2) v[r2] = r2 < CS ? cluster.map_shared_rank(Gp, r2)[idx] : 0.f;
       float s = 0.f;
-      for (int r2 = 0; r2 < CS; ++r2) s += cluster.map_shared_rank(Gp, r2)[idx];
+#pragma unroll
+      for (int r2 = 0; r2 < kNnlsMaxCluster; ++r2)
+        if (r2 < CS) s += v[r2];
       a.gram_out[idx] = s;
       Zt[idx] = s;   // reuse Zt (no longer needed) for the FP64 Hadamard sum
     }
@@ -447,9 +459,10 @@ __global__ void __launch_bounds__(W * 32, 1) nnls_cluster_kernel(const NnlsArgs 
       double h = 0.0;
       for (int idx = lane; idx < R * R; idx += 32) h = fma(np->Z[idx], (double)Zt[idx], h);
       for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xffffffffu, h, o);
+      const double mv = lane < CS ? cluster.map_shared_rank(ma, lane)[0] : 0.0;
+      double sma = 0.0;
+      for (int r2 = 0; r2 < CS; ++r2) sma += __shfl_sync(0xffffffffu, mv, r2);   // rank order
       if (lane == 0) {
-        double sma = 0.0;
-        for (int r2 = 0; r2 < CS; ++r2) sma += cluster.map_shared_rank(ma, r2)[0];
         *a.inner_MA = sma;
         *a.had_ZG = h;
         *a.iters_out = it;
